@@ -1,0 +1,273 @@
+/*
+ * pfchem.h -- C ABI of the GB300 (sm_103a) batched per-cell geochemistry library.
+ *
+ * The library replaces the body of PFLOTRAN's operator-split reaction loop:
+ *   RTReact cell loop            src/pflotran/reactive_transport.F90:1697-1724
+ *   RReact (per-cell Newton)     src/pflotran/reaction.F90:3322-3511
+ *   RTUpdateKineticState loop    src/pflotran/reactive_transport.F90:692-705
+ *   RUpdateKineticState          src/pflotran/reaction.F90:5320-5429
+ * with one batched call over all cells of a rank, executed on one GPU.
+ *
+ * Conventions
+ *  - Every table in pfchem_network has the shape and meaning of the field of
+ *    the same name in PFLOTRAN's reaction_type (src/pflotran/reaction_aux.F90:142-335,
+ *    reaction_mineral_aux.F90:76-132, reaction_surf_complex_aux.F90:68-128):
+ *    Fortran column-major, species ids 1-based, id tables dimensioned (0:ld, n)
+ *    with row 0 holding the count.  A Fortran caller passes c_loc() of its
+ *    own arrays; nothing is re-indexed on the caller side.
+ *  - Per-cell arrays are structure-of-arrays, cell fastest:
+ *    field(i, cell) lives at ptr[i * ncells + cell].
+ *  - Return codes: 0 = OK, < 0 = API or CUDA error (see pfchem_last_error),
+ *    > 0 = number of cells whose per-cell status is not PFCHEM_CELL_CONVERGED.
+ *    The library never aborts the process and never traps on the device.
+ *  - One context per host thread.  Calls are stream ordered on the context's
+ *    stream and synchronous on return.
+ */
+#ifndef PFCHEM_H
+#define PFCHEM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Compile-time limits of the device kernels (checked by pfchem_set_network). */
+#define PFCHEM_MAX_PRI 16       /* primary aqueous species (naqcomp)          */
+#define PFCHEM_MAX_CPLX 64      /* aqueous complexes (neqcplx)                */
+#define PFCHEM_MAX_MNRL 16      /* kinetic minerals (nkinmnrl)                */
+#define PFCHEM_MAX_IONX 8       /* ion-exchange reactions (neqionxrxn)        */
+#define PFCHEM_MAX_SRFRXN 8     /* surface-complexation reactions             */
+#define PFCHEM_MAX_SRFCPLX 32   /* surface complexes (nsrfcplx)               */
+#define PFCHEM_MAX_NNZ 8        /* species per reaction (leading dimensions)  */
+#define PFCHEM_MAX_PREF 4       /* rate prefactors per mineral                */
+#define PFCHEM_MAX_PREF_SPEC 4  /* species per prefactor                      */
+
+/* reaction_aux.F90:23-27 */
+#define PFCHEM_ACT_COEF_FREQUENCY_OFF 0
+#define PFCHEM_ACT_COEF_FREQUENCY_TIMESTEP 1
+#define PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER 2
+#define PFCHEM_ACT_COEF_ALGORITHM_LAG 3
+#define PFCHEM_ACT_COEF_ALGORITHM_NEWTON 4
+
+/* reaction_surf_complex_aux.F90:19-22 */
+#define PFCHEM_NULL_SURFACE 0
+#define PFCHEM_COLLOID_SURFACE 1 /* rejected: colloids are not supported      */
+#define PFCHEM_MINERAL_SURFACE 2
+#define PFCHEM_ROCK_SURFACE 3
+
+/* Residual convergence test (pfchem_options.residual_tol_kind). */
+#define PFCHEM_RESIDUAL_ABSOLUTE 0 /* max_j |F_j| < tol, F in mol/s (reaction.F90:3443) */
+#define PFCHEM_RESIDUAL_RELATIVE 1 /* max_j |F_j| / S_j < tol, S_j = magnitude of the terms of F_j */
+
+/* Accumulation convention (pfchem_options.accum_mode). */
+#define PFCHEM_ACCUM_DT_CONSISTENT 0 /* F = (psv*T(m) + V*S(m) - fixed)/dt + R(m): the global-implicit cell equation */
+#define PFCHEM_ACCUM_LITERAL 1       /* F = psv*T(m) + V*S(m) - fixed + R(m): RReact as written (reaction.F90:3424-3426) */
+
+/* Per-cell status codes. */
+#define PFCHEM_CELL_CONVERGED 0
+#define PFCHEM_CELL_MAXITER 1      /* Newton iteration cap reached            */
+#define PFCHEM_CELL_SINGULAR 2     /* a Jacobian row is zero (utility.F90:423) */
+#define PFCHEM_CELL_NONFINITE 3    /* NaN/Inf in residual or update           */
+#define PFCHEM_CELL_INNER_MAXITER 4 /* ion-exchange / surface-complexation / activity inner loop cap */
+#define PFCHEM_CELL_INACTIVE 5     /* skipped (patch%imat <= 0, reactive_transport.F90:1699) */
+
+typedef struct pfchem_network {
+  /* counts */
+  int32_t naqcomp;       /* reaction%naqcomp                                   */
+  int32_t neqcplx;       /* reaction%neqcplx                                   */
+  int32_t nkinmnrl;      /* reaction%mineral%nkinmnrl                          */
+  int32_t neqionxrxn;    /* reaction%neqionxrxn                                */
+  int32_t nsrfcplxrxn;   /* surface_complexation%nsrfcplxrxn (all equilibrium) */
+  int32_t nsrfcplx;      /* surface_complexation%nsrfcplx                      */
+  /* leading dimensions: id tables are (0:ld, n), stoich tables are (ld, n) */
+  int32_t eqcplx_ld;
+  int32_t kinmnrl_ld;
+  int32_t eqionx_ld;
+  int32_t srfcplxrxn_ld; /* srfcplxrxn_to_complex is (0:srfcplxrxn_ld, nsrfcplxrxn) */
+  int32_t srfcplx_ld;
+  int32_t max_num_prefactors;        /* size(kinmnrl_pref_rate,1); 0 = none  */
+  int32_t max_num_prefactor_species; /* size(kinmnrl_pref_alpha,1)            */
+  int32_t reserved0;
+
+  /* primary species (reaction_aux.F90 primary_spec_Z/_a0) */
+  const double *primary_spec_Z;  /* (naqcomp) */
+  const double *primary_spec_a0; /* (naqcomp) ion size [Angstrom] */
+
+  /* aqueous complexes */
+  const int32_t *eqcplxspecid;    /* (0:eqcplx_ld, neqcplx) */
+  const double *eqcplxstoich;     /* (eqcplx_ld, neqcplx) */
+  const int32_t *eqcplxh2oid;     /* (neqcplx) or NULL */
+  const double *eqcplxh2ostoich;  /* (neqcplx) or NULL */
+  const double *eqcplx_Z;         /* (neqcplx) */
+  const double *eqcplx_a0;        /* (neqcplx) */
+  const double *eqcplx_logK;      /* (neqcplx): used when use_isothermal */
+  const double *eqcplx_logKcoef;  /* (5, neqcplx) Maier-Kelly: used when !use_isothermal */
+
+  /* Debye-Hueckel parameters at the reference temperature (reaction_database.F90:897-990) */
+  double debyeA, debyeB, debyeBdot;
+
+  /* kinetic minerals (reaction_mineral_aux.F90) */
+  const int32_t *kinmnrlspecid;    /* (0:kinmnrl_ld, nkinmnrl) */
+  const double *kinmnrlstoich;     /* (kinmnrl_ld, nkinmnrl) */
+  const int32_t *kinmnrlh2oid;     /* (nkinmnrl) or NULL */
+  const double *kinmnrlh2ostoich;  /* (nkinmnrl) or NULL */
+  const double *kinmnrl_logK;      /* (nkinmnrl) */
+  const double *kinmnrl_logKcoef;  /* (5, nkinmnrl) */
+  const double *kinmnrl_rate_constant;      /* [mol/m^2/s] */
+  const double *kinmnrl_activation_energy;  /* [J/mol]; 0 = no Arrhenius factor */
+  const double *kinmnrl_molar_vol;          /* [m^3/mol] */
+  const double *kinmnrl_affinity_threshold; /* 0 = off */
+  const double *kinmnrl_rate_limiter;       /* 0 = off */
+  const double *kinmnrl_Temkin_const;       /* NULL = not associated */
+  const double *kinmnrl_min_scale_factor;   /* NULL = not associated */
+  const double *kinmnrl_affinity_power;     /* NULL = not associated */
+  const int32_t *kinmnrl_num_prefactors;    /* (nkinmnrl) or NULL */
+  const double *kinmnrl_pref_rate;              /* (max_pref, nkinmnrl) */
+  const double *kinmnrl_pref_activation_energy; /* (max_pref, nkinmnrl) */
+  const int32_t *kinmnrl_prefactor_id;          /* (0:max_pref_spec, max_pref, nkinmnrl); <0 = secondary */
+  const double *kinmnrl_pref_alpha;             /* (max_pref_spec, max_pref, nkinmnrl) */
+  const double *kinmnrl_pref_beta;
+  const double *kinmnrl_pref_atten_coef;
+
+  /* equilibrium ion exchange */
+  const int32_t *eqionx_rxn_cationid; /* (0:eqionx_ld, neqionxrxn); entry 1 = reference cation */
+  const double *eqionx_rxn_k;         /* (eqionx_ld, neqionxrxn) */
+  const double *eqionx_rxn_CEC;       /* (neqionxrxn) [eq/m^3 bulk] */
+  const int32_t *eqionx_rxn_to_surf;  /* (neqionxrxn) mineral id or 0 */
+  const int32_t *eqionx_rxn_Z_flag;   /* (neqionxrxn) logical: charges differ */
+
+  /* equilibrium surface complexation */
+  const int32_t *srfcplxrxn_to_complex;   /* (0:srfcplxrxn_ld, nsrfcplxrxn) */
+  const int32_t *srfcplxrxn_surf_type;    /* (nsrfcplxrxn) PFCHEM_*_SURFACE */
+  const int32_t *srfcplxrxn_to_surf;      /* (nsrfcplxrxn) mineral id for MINERAL_SURFACE */
+  const double *srfcplxrxn_site_density;  /* (nsrfcplxrxn) */
+  const int32_t *srfcplxrxn_stoich_flag;  /* (nsrfcplxrxn) logical */
+  const int32_t *srfcplxspecid;           /* (0:srfcplx_ld, nsrfcplx) */
+  const double *srfcplxstoich;            /* (srfcplx_ld, nsrfcplx) */
+  const int32_t *srfcplxh2oid;            /* (nsrfcplx) or NULL */
+  const double *srfcplxh2ostoich;         /* (nsrfcplx) or NULL */
+  const double *srfcplx_free_site_stoich; /* (nsrfcplx) */
+  const double *srfcplx_logK;             /* (nsrfcplx) */
+  const double *srfcplx_logKcoef;         /* (5, nsrfcplx) */
+} pfchem_network;
+
+typedef struct pfchem_options {
+  int32_t use_log_formulation;        /* reaction%use_log_formulation */
+  int32_t act_coef_update_frequency;  /* PFCHEM_ACT_COEF_FREQUENCY_* */
+  int32_t act_coef_update_algorithm;  /* PFCHEM_ACT_COEF_ALGORITHM_* */
+  int32_t use_activity_h2o;           /* reaction%use_activity_h2o */
+  int32_t use_isothermal;             /* option%use_isothermal: 1 = logK tables as given */
+  int32_t residual_tol_kind;          /* PFCHEM_RESIDUAL_* */
+  int32_t accum_mode;                 /* PFCHEM_ACCUM_* */
+  int32_t max_iterations;             /* Newton cap (the reference has none) */
+  double max_dlnC;                    /* reaction%max_dlnC (5) */
+  double max_relative_change_tolerance; /* reaction%max_relative_change_tolerance (1e-6); <= 0 disables */
+  double max_residual_tolerance;      /* reaction%max_residual_tolerance (1e-12) */
+  int32_t update_kinetic_state;       /* 1: fuse RUpdateKineticState after the solve */
+  int32_t reserved1;
+} pfchem_options;
+
+/* One batch of cells.  Pointers are all device pointers (on_device = 1) or all
+ * host pointers (on_device = 0; the library stages them through the device).
+ * Arrays marked "or NULL" may be omitted. */
+typedef struct pfchem_cells {
+  int64_t ncells;
+  int32_t on_device;
+  int32_t reserved2;
+  /* inputs (ncells) */
+  const double *temperature;            /* global_auxvar%temp [C] */
+  const double *saturation;             /* global_auxvar%sat(1) */
+  const double *den_kg;                 /* global_auxvar%den_kg(1) [kg/m^3] */
+  const double *porosity;               /* material_auxvar%porosity */
+  const double *volume;                 /* material_auxvar%volume [m^3] */
+  const double *soil_particle_density;  /* material_auxvar%soil_particle_density [kg/m^3] or NULL */
+  const int32_t *active;                /* patch%imat > 0 per cell, or NULL = all active */
+  const double *total;                  /* (naqcomp, ncells) transported totals tran_xx [mol/L] */
+  /* state, read and written (the reactive_transport_auxvar_type fields) */
+  double *pri_molal;                    /* (naqcomp, ncells) guess in, free-ion molality out */
+  double *ionic_strength;               /* (ncells) I of the previous state in (LAG activity), I at the solution out */
+  double *ln_act_h2o;                   /* (ncells) or NULL */
+  double *mnrl_volfrac;                 /* (nkinmnrl, ncells) */
+  double *mnrl_area;                    /* (nkinmnrl, ncells) [m^2/m^3 bulk] */
+  double *total_sorb_eq;                /* (naqcomp, ncells) [mol/m^3 bulk] or NULL without sorption */
+  double *eqionx_ref_cation_sorbed_conc;/* (neqionxrxn, ncells) or NULL */
+  double *srfcplxrxn_free_site_conc;    /* (nsrfcplxrxn, ncells) or NULL */
+  /* outputs */
+  double *total_out;                    /* (naqcomp, ncells) aqueous totals at the solution [mol/L] or NULL */
+  double *mnrl_rate;                    /* (nkinmnrl, ncells) [mol/m^3/s] or NULL */
+  double *sec_molal;                    /* (neqcplx, ncells) or NULL */
+  int32_t *iterations;                  /* (ncells) Newton iterations, or NULL */
+  int32_t *status;                      /* (ncells) PFCHEM_CELL_*, or NULL */
+  /* optional second initial guess (e.g. the learned warm start): the kernel
+   * evaluates the residual at both guesses and starts from the better one */
+  const double *alt_guess;              /* (naqcomp, ncells) or NULL */
+} pfchem_cells;
+
+typedef struct pfchem_stats {
+  int64_t ncells;          /* cells processed by the last call        */
+  int64_t sum_iterations;  /* sum of Newton iterations                */
+  int32_t max_iterations;  /* max Newton iterations in a cell         */
+  int32_t nonconverged;    /* cells with status != CONVERGED/INACTIVE */
+  int64_t alt_guess_used;  /* cells that started from alt_guess       */
+  double kernel_ms;        /* device time of the solve kernel         */
+} pfchem_stats;
+
+typedef struct pfchem_ctx pfchem_ctx;
+
+/* Context lifetime.  The context owns its CUDA stream, the device copy of the
+ * network tables, the work-queue counters, captured graphs and the autotune
+ * cache.  Replaces nothing in the reference (PFLOTRAN keeps this state in
+ * reaction_type and the rt_auxvars). */
+int pfchem_create(pfchem_ctx **ctx, int device);
+void pfchem_destroy(pfchem_ctx *ctx);
+const char *pfchem_last_error(const pfchem_ctx *ctx);
+
+/* Copies the reaction tables to the device.  Replaces the reaction_type
+ * object that RReact reads (reaction_aux.F90:142-335) and the per-cell
+ * RUpdateTempDependentCoefs mutation of it (reaction.F90:5433-5524): the
+ * kernels evaluate log K at each cell's temperature privately. */
+int pfchem_set_network(pfchem_ctx *ctx, const pfchem_network *net,
+                       const pfchem_options *opt);
+
+/* Batched RReact over all cells (reaction.F90:3322-3511), replacing the cell
+ * loop of RTReact (reactive_transport.F90:1697-1724); with
+ * opt.update_kinetic_state it also applies RUpdateKineticState
+ * (reaction.F90:5320-5429) to each cell.  dt = option%tran_dt [s]. */
+int pfchem_react_batch(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+/* RTReact's own layout: tran_xx holds ncomp values per cell, interleaved
+ * ((cell)*ncomp + i, reactive_transport.F90:1701-1703).  The totals are read
+ * from tran_xx (cells->total is ignored); on return the first naqcomp entries
+ * of each cell hold the free-ion molalities, as RTReact writes back at
+ * reactive_transport.F90:1711.  The guess/state pri_molal and every other
+ * per-cell field come from `cells` as in pfchem_react_batch.  tran_xx is a
+ * pointer of the same kind (host or device) as the others. */
+int pfchem_react_batch_interleaved(pfchem_ctx *ctx, double dt, int32_t ncomp,
+                                   double *tran_xx, pfchem_cells *cells);
+
+/* Batched RUpdateKineticState (reaction.F90:5320-5429) at the current state,
+ * replacing the cell loop of RTUpdateKineticState (reactive_transport.F90:692-705). */
+int pfchem_update_kinetic_state(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+/* Statistics of the last react call: what the OS_STATISTICS block of RTReact
+ * accumulates (reactive_transport.F90:1645-1804). */
+int pfchem_last_stats(const pfchem_ctx *ctx, pfchem_stats *stats);
+
+/* Kernel mapping chosen by the autotuner or forced by the caller. */
+typedef struct pfchem_launch {
+  int32_t block_threads;    /* threads per block                         */
+  int32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid */
+  int32_t refill_min_idle;  /* lanes idle in a warp before they fetch new cells */
+  int32_t reserved3;
+} pfchem_launch;
+int pfchem_get_launch(const pfchem_ctx *ctx, pfchem_launch *launch);
+int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
+/* Times candidate mappings on `cells` (device pointers; the state arrays are
+ * restored after every trial) and keeps the fastest. */
+int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PFCHEM_H */

@@ -1,0 +1,377 @@
+"""Seeded synthetic workloads for the per-cell chemistry step.
+
+Three workloads, each a (network, options, cells, dt) tuple:
+
+* calcite column (100 cells, 25 C, dt 3600 s): the calcite system of
+  PFLOTRAN's regression tests (regression_tests/ascem/batch/calcite.dat),
+  primaries H+, HCO3-, Ca++; complexes OH-, CO3--, CO2(aq), CaCO3(aq),
+  CaHCO3+; kinetic calcite (k 1e-9 mol/m^2/s, area 1 m^2/m^3, volume
+  fraction 1e-5).  Totals: Ca and carbonate log-uniform in [1e-5, 1e-2] M,
+  pH uniform in [5, 9].
+* calcite grid (100^3 cells, dt 1 day): the same network with T uniform in
+  [10, 60] C and log K linear in T between the 25 C values and 60 C values
+  offset by +-0.3 (seeded), i.e. Maier-Kelly coefficients (0, a, b, 0, 0).
+* synthetic 12-species network (2M cells, dt 1 day): 40 aqueous complexes, 6
+  kinetic minerals, 4 ion-exchange reactions (CEC 5 meq/100 g) and 2
+  surface-complexation reactions, stoichiometry in {-2..2} with ~3 nonzeros,
+  log K in [-15, 15], rate constants log-uniform in [1e-12, 1e-6].  Cells
+  start at an equilibrium state (forward speciation of seeded free-ion
+  molalities whose totals lie in [1e-10, 1e-1] M) and take a seeded
+  log-normal "transport update" of their totals, which spreads the Newton
+  iteration count over ~2-40.
+
+Everything is generated on the host with numpy from numpy.random.Generator
+(PCG64) streams, so a seed fixes the inputs on any machine up to the last
+ulp of numpy's exp/log.  The forward speciation here is host-side input
+generation; it restates RTotal/RTotalSorb only to build consistent states.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import abi
+from .cells import CellBatch
+from .network import ReactionNetwork, default_options
+
+LOG_TO_LN = 2.30258509299  # pflotran_constants.F90:48
+# IFC67 liquid density at 25 C and 101325 Pa: the reference_water_density a
+# transport-only PFLOTRAN run uses (factory_subsurface.F90:995-1000).
+DEN_KG_25C = 997.1604062672549
+
+
+# ---------------------------------------------------------------------------
+# networks
+
+def calcite_network(temperature_dependent=False, seed=0, delta=0.3):
+    """Calcite network; with temperature_dependent, log K(T) is linear in T_K
+    between 25 C and 60 C with a seeded +-delta offset at 60 C."""
+    net = ReactionNetwork([("H+", 1.0, 9.0), ("HCO3-", -1.0, 4.0), ("Ca++", 2.0, 6.0)])
+    rng = np.random.default_rng(seed + 7919)
+
+    def coef(logK25):
+        if not temperature_dependent:
+            return None
+        d = delta if rng.random() < 0.5 else -delta
+        t1, t2 = 298.15, 333.15
+        b = d / (t2 - t1)
+        a = logK25 - b * t1
+        return (0.0, a, b, 0.0, 0.0)
+
+    # calcite.dat rows (stoichiometry, 25 C log K, a0)
+    net.add_complex("OH-", {"H+": -1.0}, 13.9951, a0=3.5, h2o=1.0, logKcoef=coef(13.9951))
+    net.add_complex("CO3--", {"H+": -1.0, "HCO3-": 1.0}, 10.3288, a0=4.5, logKcoef=coef(10.3288))
+    net.add_complex("CO2(aq)", {"H+": 1.0, "HCO3-": 1.0}, -6.3447, a0=3.0, h2o=-1.0, logKcoef=coef(-6.3447))
+    net.add_complex("CaCO3(aq)", {"H+": -1.0, "Ca++": 1.0, "HCO3-": 1.0}, 7.0017, a0=3.0, logKcoef=coef(7.0017))
+    net.add_complex("CaHCO3+", {"Ca++": 1.0, "HCO3-": 1.0}, -1.0467, a0=4.0, logKcoef=coef(-1.0467))
+    net.add_kinetic_mineral("Calcite", {"H+": -1.0, "Ca++": 1.0, "HCO3-": 1.0}, 1.8487,
+                            rate_constant=1e-9, molar_vol=36.934e-6, logKcoef=coef(1.8487))
+    net.build()
+    return net
+
+
+def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rho_s=2650.0):
+    """Seeded synthetic network with the sizes of the 12-species workload."""
+    rng = np.random.default_rng(seed)
+    # charges: >= 4 cations (Z > 0) for ion exchange, the rest in {-2..2}
+    Z = np.array([1, 2, 1, 2, 1, -1, -2, -1, 0, 1, -1, 2], dtype=float)[:N]
+    rng.shuffle(Z)
+    a0 = rng.uniform(3.0, 9.0, N)
+    names = [f"P{i}" for i in range(N)]
+    net = ReactionNetwork([(names[i], Z[i], a0[i]) for i in range(N)])
+    lm_ref = np.log(1e-5)
+
+    def draw_rxn(nnz_choices=(2, 3, 3, 4), lo=-14.0, hi=-3.0, force_pos=True):
+        while True:
+            nnz = int(rng.choice(nnz_choices))
+            sp = rng.choice(N, nnz, replace=False)
+            nu = rng.choice([-2, -1, 1, 2], nnz, p=[0.15, 0.2, 0.45, 0.2]).astype(float)
+            if force_pos and nu.max() <= 0:
+                continue
+            logK = rng.uniform(-15.0, 15.0)
+            # keep reactions whose species concentration at the reference
+            # state (all free ions 1e-5 mol/kg) lies in [10^lo, 10^hi]
+            log10C = -logK + nu.sum() * lm_ref / LOG_TO_LN
+            if lo <= log10C <= hi:
+                return sp, nu, logK
+
+    for i in range(Nc):
+        sp, nu, logK = draw_rxn()
+        net.add_complex(f"C{i}", {names[s]: v for s, v in zip(sp, nu)}, logK, a0=rng.uniform(3.0, 9.0))
+    for m in range(Nm):
+        sp, nu, logK = draw_rxn(nnz_choices=(2, 3, 3, 4), lo=-2.0, hi=2.0)
+        k = 10.0 ** rng.uniform(-12.0, -6.0)
+        net.add_kinetic_mineral(f"M{m}", {names[s]: v for s, v in zip(sp, nu)}, logK,
+                                rate_constant=k, molar_vol=30e-6)
+    cations = [i for i in range(N) if Z[i] > 0]
+    # CEC 5 meq/100 g = 0.05 eq/kg solid -> eq/m^3 bulk (reaction.F90:657-660)
+    CEC = 0.05 * rho_s * (1.0 - porosity)
+    for r in range(Nix):
+        sp = rng.choice(cations, 3, replace=False)
+        ks = [1.0] + list(10.0 ** rng.uniform(-1.0, 1.0, 2))
+        net.add_ion_exchange([(names[s], k) for s, k in zip(sp, ks)], CEC)
+    for r in range(Nsr):
+        cx = []
+        for j in range(3):
+            nnz = int(rng.choice([1, 2]))
+            sp = rng.choice(N, nnz, replace=False)
+            nu = rng.choice([-1, 1, 2], nnz, p=[0.3, 0.5, 0.2]).astype(float)
+            while True:
+                logK = rng.uniform(-15.0, 15.0)
+                # surface complex / free site ratio at the reference state in [1e-3, 1e1]
+                lr = -logK + nu.sum() * lm_ref / LOG_TO_LN
+                if -3.0 <= lr <= 1.0:
+                    break
+            cx.append(({names[s]: v for s, v in zip(sp, nu)}, 1.0, logK))
+        stype = abi.ROCK_SURFACE if r == 0 else abi.NULL_SURFACE
+        dens = 1e-3 if stype == abi.ROCK_SURFACE else 1.0  # mol/kg solid (rock) / mol/m^3 (null)
+        net.add_surface_complexation(dens, cx, surf_type=stype)
+    net.build()
+    return net
+
+
+# ---------------------------------------------------------------------------
+# host-side forward speciation (input generation)
+
+class Speciator:
+    """Vectorised RTotal / RTotalSorb at given free-ion molalities."""
+
+    def __init__(self, net: ReactionNetwork):
+        self.net = net
+        t = net._tables if net._tables is not None else net.build()
+        self.t = t
+        N, Nc = net.N, net.Nc
+        self.nu = np.zeros((Nc, N))
+        ld = t["eqcplx_ld"]
+        ids = t["eqcplxspecid"].reshape(-1, ld + 1)
+        st = t["eqcplxstoich"].reshape(-1, ld)
+        for i in range(Nc):
+            for k in range(ids[i, 0]):
+                self.nu[i, ids[i, k + 1] - 1] = st[i, k]
+        self.h2o = t["eqcplxh2ostoich"][:Nc]
+        self.Zp, self.Zc = t["primary_spec_Z"], t["eqcplx_Z"][:Nc]
+        self.ap, self.ac = t["primary_spec_a0"], t["eqcplx_a0"][:Nc]
+        self.coef = t["eqcplx_logKcoef"].reshape(-1, 5)[:Nc]
+        self.logK = t["eqcplx_logK"][:Nc]
+
+    def logK_at(self, T, isothermal):
+        if isothermal:
+            return np.broadcast_to(self.logK, (len(T), len(self.logK)))
+        tk = (T + 273.15)[:, None]
+        c = self.coef
+        return c[:, 0] * np.log(tk) + c[:, 1] + c[:, 2] * tk + c[:, 3] / tk + c[:, 4] / (tk * tk)
+
+    def ln_gamma(self, I):
+        """LAG activity coefficients (reaction.F90:3992-4051) as ln gamma."""
+        A, B, Bd = self.net.debye
+        s = np.sqrt(I)[:, None]
+        lp = (-self.Zp ** 2 * s * A / (1.0 + self.ap * B * s) + Bd * I[:, None]) * LOG_TO_LN
+        lc = (-self.Zc ** 2 * s * A / (1.0 + self.ac * B * s) + Bd * I[:, None]) * LOG_TO_LN
+        lp = np.where(np.abs(self.Zp) > 1e-10, lp, 0.0)
+        lc = np.where(np.abs(self.Zc) > 1e-10, lc, 0.0)
+        return lp, lc
+
+    def aqueous(self, lnm, logK, lngp, lngc):
+        """molal totals Psi (n,N), complexes C (n,Nc)."""
+        ln_act = lnm + lngp
+        lnQK = -logK * LOG_TO_LN + ln_act @ self.nu.T
+        Cc = np.exp(lnQK - lngc)
+        Psi = np.exp(lnm) + Cc @ self.nu
+        return Psi, Cc
+
+    def ionic_strength(self, lnm, Cc):
+        return 0.5 * (np.exp(lnm) @ (self.Zp ** 2) + Cc @ (self.Zc ** 2))
+
+    def sorbed(self, m, gp, mnrl_volfrac, porosity, rho_s, ref_sorbed0=1e-9, free_site0=1e-9, logKsc=None):
+        """Equilibrium sorbed totals (mol/m^3 bulk) and the sorption warm
+        starts, following RTotalSorbEqIonx (reaction.F90:4305-4535) and
+        RTotalSorbEqSurfCplx1 (reaction_surf_complex.F90:658-934)."""
+        net, t = self.net, self.t
+        n, N = m.shape
+        S = np.zeros((n, N))
+        ref_out = np.zeros((n, net.Nix))
+        a = m * gp
+        ldx = t["eqionx_ld"]
+        xid = t["eqionx_rxn_cationid"].reshape(-1, ldx + 1)
+        xk = t["eqionx_rxn_k"].reshape(-1, ldx)
+        for r in range(net.Nix):
+            nc = xid[r, 0]
+            ids = xid[r, 1:nc + 1] - 1
+            ks = xk[r, :nc]
+            Zs = self.Zp[ids]
+            to = t["eqionx_rxn_to_surf"][r]
+            omega = t["eqionx_rxn_CEC"][r] * (np.maximum(mnrl_volfrac[:, to - 1], 1e-40) if to > 0 else 1.0)
+            omega = np.broadcast_to(omega, (n,))
+            if t["eqionx_rxn_Z_flag"][r]:
+                ref = ks[0] * a[:, ids[0]]
+                KD = (Zs[0] * ref_sorbed0 / omega) / ref
+                for _ in range(200):
+                    tot = KD * ref
+                    d = ref.copy()
+                    for j in range(1, nc):
+                        x = ks[j] * a[:, ids[j]] * KD ** (Zs[j] / Zs[0])
+                        tot = tot + x
+                        d = d + x / KD * Zs[j] / Zs[0]
+                    step = (1.0 - tot) / d
+                    KD = np.maximum(KD + step, 1e-40)
+                    if np.all(np.abs(step / KD) < 1e-13):
+                        break
+                X = [KD * ref] + [ks[j] * a[:, ids[j]] * KD ** (Zs[j] / Zs[0]) for j in range(1, nc)]
+                ref_out[:, r] = X[0] * omega / Zs[0]
+            else:
+                X = [ks[j] * a[:, ids[j]] for j in range(nc)]
+                s = sum(X)
+                X = [x / s for x in X]
+                ref_out[:, r] = ref_sorbed0
+            for j in range(nc):
+                S[:, ids[j]] += X[j] * omega / Zs[j]
+        free_out = np.zeros((n, net.Nsr))
+        ldr, lds = t["srfcplxrxn_ld"], t["srfcplx_ld"]
+        r2c = t["srfcplxrxn_to_complex"].reshape(-1, ldr + 1)
+        sid = t["srfcplxspecid"].reshape(-1, lds + 1)
+        sst = t["srfcplxstoich"].reshape(-1, lds)
+        lnact = np.log(a)
+        for r in range(net.Nsr):
+            stype = t["srfcplxrxn_surf_type"][r]
+            dens = t["srfcplxrxn_site_density"][r]
+            if stype == abi.ROCK_SURFACE:
+                site = dens * rho_s * (1.0 - porosity)
+            elif stype == abi.MINERAL_SURFACE:
+                site = dens * mnrl_volfrac[:, t["srfcplxrxn_to_surf"][r] - 1]
+            else:
+                site = np.full(n, dens)
+            site = np.broadcast_to(site, (n,))
+            terms = []
+            for j in range(r2c[r, 0]):
+                ic = r2c[r, j + 1] - 1
+                lq = -t["srfcplx_logK"][ic] * LOG_TO_LN
+                lq = lq + sum(sst[ic, k] * lnact[:, sid[ic, k + 1] - 1] for k in range(sid[ic, 0]))
+                terms.append((ic, lq))
+            # free-site stoichiometry 1: closed form Sx = site / (1 + sum K_i a^nu)
+            ratio = sum(np.exp(lq) for _, lq in terms)
+            free = site / (1.0 + ratio)
+            free_out[:, r] = free
+            for ic, lq in terms:
+                Sc = np.exp(lq) * free
+                for k in range(sid[ic, 0]):
+                    S[:, sid[ic, k + 1] - 1] += sst[ic, k] * Sc
+        return S, ref_out, free_out
+
+
+def _fill_common(b, n, porosity=0.25, sat=1.0, volume=1.0, den=DEN_KG_25C, rho_s=2650.0):
+    b.saturation[:] = sat
+    b.porosity[:] = porosity
+    b.volume[:] = volume
+    b.den_kg[:] = den
+    b.soil_particle_density[:] = rho_s
+
+
+def calcite_cells(n=100, seed=0, temperature_dependent=False, net=None):
+    """Calcite column (25 C) or, with temperature_dependent, the calcite grid
+    workload with T ~ U[10, 60] C.  Returns (net, opt, cells, dt)."""
+    rng = np.random.default_rng(seed)
+    if net is None:
+        net = calcite_network(temperature_dependent=temperature_dependent, seed=seed)
+    opt = default_options(use_isothermal=0 if temperature_dependent else 1)
+    sp = Speciator(net)
+    b = CellBatch.allocate(net, n)
+    _fill_common(b, n)
+    T = rng.uniform(10.0, 60.0, n) if temperature_dependent else np.full(n, 25.0)
+    b.temperature[:] = T
+    tCa = 10.0 ** rng.uniform(-5.0, -2.0, n)
+    tC = 10.0 ** rng.uniform(-5.0, -2.0, n)
+    pH = rng.uniform(5.0, 9.0, n)
+    den_L = b.den_kg * 1e-3
+    logK = sp.logK_at(T, opt.use_isothermal)
+    # constraint speciation: pH row for H+, TOTAL rows for HCO3- and Ca++
+    lnm = np.stack([-pH * LOG_TO_LN, np.log(tC / den_L), np.log(tCa / den_L)], axis=1)
+    I = np.full(n, 1e-3)
+    for outer in range(30):
+        lngp, lngc = sp.ln_gamma(I)
+        lnm[:, 0] = -pH * LOG_TO_LN - lngp[:, 0]
+        for it in range(60):
+            Psi, Cc = sp.aqueous(lnm, logK, lngp, lngc)
+            F = Psi[:, 1:] * den_L[:, None] - np.stack([tC, tCa], 1)
+            # d Psi_j / d ln m_k = m_j delta_jk + sum_i nu_ij nu_ik C_i
+            Jf = np.einsum("ij,ik,ni->njk", sp.nu, sp.nu, Cc) + np.einsum("jk,nj->njk", np.eye(3), np.exp(lnm))
+            J = Jf[:, 1:, 1:] * den_L[:, None, None]
+            d = np.linalg.solve(J, F[..., None])[..., 0]
+            d = np.clip(d, -2.0, 2.0)
+            lnm[:, 1:] -= d
+            if np.max(np.abs(d)) < 1e-14:
+                break
+        Inew = sp.ionic_strength(lnm, Cc)
+        if np.max(np.abs(Inew - I) / Inew) < 1e-15:
+            I = Inew
+            break
+        I = Inew
+    lngp, lngc = sp.ln_gamma(I)
+    Psi, Cc = sp.aqueous(lnm, logK, lngp, lngc)
+    b.view("total", net.N)[:] = (Psi * den_L[:, None]).T
+    b.view("pri_molal", net.N)[:] = np.exp(lnm).T
+    b.ionic_strength[:] = sp.ionic_strength(lnm, Cc)
+    b.mnrl_volfrac[:] = 1e-5
+    b.mnrl_area[:] = 1.0
+    dt = 86400.0 if temperature_dependent else 3600.0
+    return net, opt, b, dt
+
+
+def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-3, 3.0), tot_range=(1e-10, 1e-1)):
+    """Cells of the synthetic 12-species workload.  Returns (net, opt, cells, dt)."""
+    if net is None:
+        net = synthetic_network()
+    rng = np.random.default_rng(seed)
+    opt = default_options(use_isothermal=1)
+    sp = Speciator(net)
+    N = net.N
+    porosity, rho_s = 0.25, 2650.0
+    lnm = np.empty((0, N))
+    have = 0
+    chunks = []
+    while have < n:
+        k = max(2 * (n - have), 1024)
+        cand = rng.uniform(np.log(1e-9), np.log(2e-3), (k, N))
+        I0 = np.full(k, 1e-2)
+        for _ in range(8):
+            lngp, lngc = sp.ln_gamma(I0)
+            Psi, Cc = sp.aqueous(cand, sp.logK, lngp, lngc)
+            I0 = sp.ionic_strength(cand, Cc)
+        tot = Psi * DEN_KG_25C * 1e-3
+        ok = np.all((tot >= tot_range[0]) & (tot <= tot_range[1]), axis=1) & (I0 < 1.0)
+        chunks.append(cand[ok])
+        have += int(ok.sum())
+    lnm = np.concatenate(chunks)[:n]
+    b = CellBatch.allocate(net, n)
+    _fill_common(b, n, porosity=porosity, rho_s=rho_s)
+    b.temperature[:] = 25.0
+    den_L = b.den_kg * 1e-3
+    # self-consistent ionic strength of the equilibrium state
+    I = np.full(n, 1e-2)
+    for _ in range(60):
+        lngp, lngc = sp.ln_gamma(I)
+        Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
+        Inew = sp.ionic_strength(lnm, Cc)
+        if np.max(np.abs(Inew - I) / Inew) < 1e-15:
+            I = Inew
+            break
+        I = Inew
+    lngp, lngc = sp.ln_gamma(I)
+    Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
+    m = np.exp(lnm)
+    vf = np.full((n, max(net.Nm, 1)), 1e-3)
+    S, ref, free = sp.sorbed(m, np.exp(lngp), vf, porosity, rho_s)
+    # seeded log-normal transport update of the totals
+    sig = 10.0 ** rng.uniform(np.log10(sigma_range[0]), np.log10(sigma_range[1]), n)
+    xi = rng.standard_normal((n, N))
+    tot_eq = Psi * den_L[:, None]
+    b.view("total", N)[:] = (tot_eq * np.exp(sig[:, None] * xi)).T
+    b.view("pri_molal", N)[:] = m.T
+    b.ionic_strength[:] = sp.ionic_strength(lnm, Cc)
+    b.mnrl_volfrac[:] = 1e-3
+    b.mnrl_area[:] = 1.0
+    if net.Nix + net.Nsr > 0:
+        b.view("total_sorb_eq", N)[:] = S.T
+    if net.Nix > 0:
+        b.view("eqionx_ref_cation_sorbed_conc", net.Nix)[:] = ref.T
+    if net.Nsr > 0:
+        b.view("srfcplxrxn_free_site_conc", net.Nsr)[:] = free.T
+    return net, opt, b, 86400.0

@@ -1,0 +1,58 @@
+"""The oracle against PFLOTRAN's own known answers.
+
+Fixtures: tests/golden/*.json, written from the reference's regression decks
+and gold files by tests/golden/make_kat_fixtures.py.  The tolerances are the
+regression harness's (regression_tests/ascem/batch/batch.cfg:15-19: 1e-12
+absolute for concentrations, rates and volume fractions) unless stated.
+"""
+import numpy as np
+import pytest
+
+import kat
+
+
+def test_ifc67_density_matches_pfunit_value(oracle):
+    # src/pflotran/unittests/test_eos_water.pf:131-157 pins 998.32340486329440 kg/m^3 at 20 C
+    assert abs(oracle.ifc67_density(20.0, 101325.0) - 998.32340486329440) <= 1e-12
+
+
+def test_ion_exchange_valocchi_gold(oracle):
+    """ion-exchange-valocchi: constraint speciation + RTotalSorbEqIonx (Z != Z inner Newton)."""
+    out, gold = kat.run_ion_exchange_valocchi(oracle)
+    for key in ("Total Na+", "Total Ca++", "Total Mg++", "Total Cl-", "Total Sorbed Na+",
+                "Total Sorbed Ca++", "Total Sorbed Mg++", "Total Sorbed Cl-"):
+        assert abs(out[key] - gold[key]) <= 1e-12, (key, out[key], gold[key])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_calcite_kinetics_gold(oracle, precision):
+    """calcite-kinetics: 500 steps of 0.5 s of RTotal + LAG activity (TIMESTEP) +
+    RKineticMineral + RUpdateKineticState.  Totals, calcite volume fraction and
+    rate meet the harness's 1e-12 absolute; pH (which depends on which state's
+    ionic strength the output's activity coefficient used) is held to 5e-8."""
+    out, gold = kat.run_calcite_kinetics(oracle, precision)
+    for key in ("Total H+", "Total HCO3-", "Total Ca++", "Calcite VF", "Calcite Rate"):
+        assert abs(out[key] - gold[key]) <= 1e-12, (key, out[key], gold[key])
+    assert abs(out["pH"] - gold["pH"]) <= 5e-8
+
+
+def test_rsolve_matches_dense_solve(oracle):
+    rng = np.random.default_rng(0)
+    for n in (3, 7, 12):
+        A = rng.standard_normal((n, n)) + n * np.eye(n)
+        r = rng.standard_normal(n)
+        conc = np.exp(rng.uniform(-5, 0, n))
+        u = np.zeros(n)
+        Ac = A.copy()
+        assert oracle.lib().pfo_rsolve(n, r.copy().ctypes.data, Ac.ctypes.data, conc.ctypes.data, 1, u.ctypes.data) == 0
+        ref = np.linalg.solve(A * conc[None, :], r)
+        assert np.allclose(u, ref, rtol=1e-10, atol=1e-12)
+
+
+def test_rsolve_reports_singular_row(oracle):
+    A = np.eye(3)
+    A[1, :] = 0.0
+    u = np.zeros(3)
+    r = np.ones(3)
+    c = np.ones(3)
+    assert oracle.lib().pfo_rsolve(3, r.ctypes.data, A.ctypes.data, c.ctypes.data, 0, u.ctypes.data) == 1
