@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Benchmark of the batched per-cell chemistry step on one GB300.
+
+Workload: the synthetic 12-primary-species network (40 aqueous complexes, 6
+kinetic TST minerals, 4 ion-exchange and 2 surface-complexation reactions)
+on 2,097,152 cells, FP64, dt = 1 day, converged to a 1e-12 relative
+residual.  One "step" is one reaction step over all cells.
+
+  value   converged cell solves/s with inputs resident in HBM (device time of
+          the solve, CUDA events on the library's stream, summed over the
+          timed steps; the cell state is restored from a pristine copy between
+          steps, outside the timed interval)
+  e2e     the same metric through pfchem_react_batch with pinned host
+          buffers: every step uploads inputs and state and downloads state
+          and outputs
+  cpu_baseline  the oracle (C++ restatement of RReact) on a bounded sample
+          of the same cells on all host cores
+
+`--impl reference` times the reference's CPU implementation of the step
+(the oracle port: PFLOTRAN's Fortran cannot be built in this image) on the
+same workload and prints the same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start vs plain GPU Newton"
+UNIT = "cell solves/s"
+NCELLS = 2_097_152
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="pflotran_gb300")
+    p.add_argument("--ncells", type=int, default=NCELLS)
+    p.add_argument("--cpu-sample", type=int, default=20000)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--autotune", action="store_true")
+    return p.parse_args()
+
+
+def rank_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Clocks:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        self.f.flush()
+        rows = []
+        try:
+            for line in open(self.f.name):
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def make_workload(ncells):
+    from pflotran_gb300 import workloads
+    net = workloads.synthetic_network()
+    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024, net=net)
+    return net, opt, cells, dt
+
+
+def cpu_baseline(net, opt, cells, dt, sample):
+    from oracle import oracle
+    idx = np.arange(min(sample, cells.ncells))
+    sub = cells.subset(idx, net)
+    sub.iterations = np.zeros(len(idx), np.int32)
+    sub.status = np.zeros(len(idx), np.int32)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    oracle.react(net.as_struct(), opt, dt, sub, 0, threads)
+    el = time.perf_counter() - t0
+    return {"value": len(idx) / el, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {len(idx)} cells of the {cells.ncells}-cell workload, oracle RReact in double, "
+                      f"{threads} std::threads"}, sub
+
+
+def run_reference(args):
+    rank, world, _ = rank_env()
+    if rank != 0:
+        return
+    net, opt, cells, dt = make_workload(args.ncells)
+    from oracle import oracle
+    threads = os.cpu_count() or 1
+    n = min(args.cpu_sample, cells.ncells)
+    sub0 = cells.subset(np.arange(n), net)
+    times = []
+    for s in range(args.warmup + args.steps):
+        sub = sub0.copy()
+        t0 = time.perf_counter()
+        oracle.react(net.as_struct(), opt, dt, sub, 0, threads)
+        el = time.perf_counter() - t0
+        if s >= args.warmup:
+            times.append(el)
+    value = n / (sum(times) / len(times))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"synthetic 12-species network (40 complexes, 6 minerals, 4 ion-exchange, "
+                               f"2 surface-complexation), {args.ncells} cells, dt 1 day, 1e-12 rel. residual",
+                   "sample_cells_per_step": n},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{n} of {args.ncells} cells per step (oracle C++ restatement of RReact; "
+                                   f"PFLOTRAN's Fortran cannot be compiled in this image)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    import torch
+    rank, world, local = rank_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from pflotran_gb300 import work
+    from pflotran_gb300.cells import CellBatch
+    from pflotran_gb300.lib import ReactionStep
+
+    net, opt, host, dt = make_workload(args.ncells)
+    n = host.ncells
+    step = ReactionStep(net, opt, device=local)
+    pristine = host.to_device()
+    dev = pristine.copy()
+    if args.autotune:
+        step.autotune(dev, dt)
+    launch = step.launch()
+
+    def restore():
+        for f in CellBatch.FIELDS:
+            a = getattr(pristine, f)
+            if a is not None:
+                getattr(dev, f).copy_(a)
+
+    # warm-up
+    for _ in range(args.warmup):
+        restore()
+        step.react(dev, dt)
+    torch.cuda.synchronize()
+    # timed: device time of the solve per step, summed
+    dev_ms = []
+    iters = []
+    with Clocks(local) as clk:
+        for _ in range(args.steps):
+            restore()
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            bad = step.react(dev, dt)
+            st = step.stats()
+            dev_ms.append(st.kernel_ms)
+            iters.append(st.sum_iterations)
+            torch.cuda.synchronize()
+    clocks = clk.summary()
+    total_ms = float(np.sum(dev_ms))
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step * 1e-3)
+    g = dev.to_host()
+    conv = int((g.status == 0).sum())
+
+    # end-to-end through the public API with pinned host buffers
+    pinned = CellBatch(n)
+    for f in CellBatch.FIELDS:
+        a = getattr(host, f)
+        if a is not None:
+            t = torch.empty(a.size, dtype=torch.float64 if a.dtype == np.float64 else torch.int32).pin_memory()
+            t.numpy()[:] = a
+            setattr(pinned, f, t.numpy())
+    h2d = sum(getattr(pinned, f).nbytes for f in ("temperature", "saturation", "den_kg", "porosity", "volume",
+                                                   "soil_particle_density", "total", "pri_molal", "ionic_strength",
+                                                   "mnrl_volfrac", "mnrl_area", "total_sorb_eq",
+                                                   "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc")
+              if getattr(pinned, f) is not None)
+    d2h = sum(getattr(pinned, f).nbytes for f in ("pri_molal", "ionic_strength", "mnrl_volfrac", "total_sorb_eq",
+                                                   "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc",
+                                                   "total_out", "mnrl_rate", "iterations", "status")
+              if getattr(pinned, f) is not None)
+    state_fields = ("pri_molal", "ionic_strength", "mnrl_volfrac", "total_sorb_eq",
+                    "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc")
+    e2e_s = []
+    for s in range(args.warmup + args.steps):
+        for f in state_fields:
+            a = getattr(pinned, f)
+            if a is not None:
+                a[:] = getattr(host, f)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        step.react(pinned, dt)
+        el = time.perf_counter() - t0
+        if s >= args.warmup:
+            e2e_s.append(el)
+    e2e_value = world * n / (sum(e2e_s) / len(e2e_s))
+
+    # roofline: FP64-issue bound; algorithmic flops per launch / device time
+    mean_iters = float(np.mean(iters)) / n
+    flops = work.step_flops(net, g.iterations, isothermal=bool(opt.use_isothermal))
+    achieved_tflops = flops / (ms_per_step * 1e-3) / 1e12
+    probe = fp64_peak(local)
+    bytes_step = work.bytes_per_cell(net) * n
+    hbm_gbs = bytes_step / (ms_per_step * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"synthetic 12-species network (40 complexes, 6 minerals, 4 ion-exchange, "
+                               f"2 surface-complexation), {n} cells per GPU, dt 1 day, plain Newton from the "
+                               f"previous-step guess, 1e-12 rel. residual",
+                   "ncells": n, "l2": "inputs ~1.3 GB >> L2; state restored from a pristine copy between steps",
+                   "launch": {"block_threads": launch.block_threads, "blocks_per_sm": launch.blocks_per_sm,
+                              "refill_min_idle": launch.refill_min_idle},
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "mean_newton_iterations": mean_iters, "converged_cells": conv,
+        "iteration_histogram": np.bincount(g.iterations).tolist(),
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": probe, "unit": "TFLOP/s",
+                     "frac": achieved_tflops / probe if probe else None, "traffic": None,
+                     "peak_source": "measured DFMA throughput on this GPU (pfchem_probe_fp64_peak, FMA = 2 flops)",
+                     "flops_per_step": flops,
+                     "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
+                             "bytes_per_step": bytes_step, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
+        "clocks": clocks,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+    }
+    if rank == 0 and not args.no_cpu:
+        cb, _ = cpu_baseline(net, opt, host, dt, args.cpu_sample)
+        line["cpu_baseline"] = cb
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def fp64_peak(device):
+    import ctypes as C
+    from pflotran_gb300.build import PROBE, build
+    build()
+    l = C.CDLL(PROBE)
+    l.pfchem_probe_fp64_peak.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    tf = C.c_double()
+    ms = C.c_double()
+    if l.pfchem_probe_fp64_peak(device, 4096, C.byref(tf), C.byref(ms)) != 0:
+        return None
+    return tf.value
+
+
+if __name__ == "__main__":
+    main()

@@ -242,7 +242,9 @@ int activity_coefficients(const Net &w, const pfchem_options &o, Cell<R> &c, boo
             : R(1);
     sum_sec_molal = sum_sec_molal + c.sec_molal[i];
   }
-  if (o.use_activity_h2o) {
+  // With the ionic strength taken from the state, ln a_H2O is the state's
+  // value too: both were computed at the previous solution.
+  if (o.use_activity_h2o && !use_I_start) {
     R v = R(1) - R(0.017) * (sum_pri_molal + sum_sec_molal);
     c.ln_act_h2o = v > 0 ? rlog(v) : R(0);
   }
@@ -1022,7 +1024,17 @@ void react_one(const Net &w, const pfchem_options &o, double dt, pfchem_cells *c
   for (int r = 0; r < w.Nix; ++r) cl->eqionx_ref_cation_sorbed_conc[r * n + k] = (double)c.eqionx_ref_cation_sorbed_conc[r];
   for (int r = 0; r < w.Nsr; ++r) cl->srfcplxrxn_free_site_conc[r * n + k] = (double)c.srfcplxrxn_free_site_conc[r];
   cl->ionic_strength[k] = (double)ionic_strength_of(w, c);
-  if (cl->ln_act_h2o) cl->ln_act_h2o[k] = (double)c.ln_act_h2o;
+  if (cl->ln_act_h2o) {
+    // the value RActivityCoefficients would compute at the solution (reaction.F90:4043-4050)
+    if (o.use_activity_h2o) {
+      R s = 0;
+      for (int j = 0; j < w.N; ++j) s += c.pri_molal[j];
+      for (int i = 0; i < w.Nc; ++i) s += c.sec_molal[i];
+      R v = R(1) - R(0.017) * s;
+      c.ln_act_h2o = v > 0 ? rlog(v) : R(0);
+    }
+    cl->ln_act_h2o[k] = (double)c.ln_act_h2o;
+  }
   if (cl->iterations) cl->iterations[k] = iters;
   if (cl->status) cl->status[k] = status;
 }

@@ -1,0 +1,74 @@
+"""Builds the in-tree CUDA library libpfchem.so for sm_103a with nvcc.
+
+Two translation units compiled in parallel, then linked; output in
+pflotran_gb300/_build/.  Re-running skips the build when no source changed.
+"""
+import hashlib
+import os
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "csrc")
+OUT = os.path.join(HERE, "_build")
+LIB = os.path.join(OUT, "libpfchem.so")
+PROBE = os.path.join(OUT, "libpfchem_probe.so")
+SOURCES = ["pfchem_newton.cu", "pfchem_api.cu"]
+PROBE_SOURCES = ["fp64_peak.cu"]
+HEADERS = ["pfchem_device.cuh", os.path.join("..", "..", "include", "pfchem.h")]
+NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
+
+
+def _nvcc():
+    for c in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if c and (os.path.sep not in c or os.path.exists(c)):
+            return c
+    return "nvcc"
+
+
+def _digest():
+    h = hashlib.sha256()
+    for f in SOURCES + PROBE_SOURCES + HEADERS:
+        with open(os.path.join(CSRC, f), "rb") as fh:
+            h.update(fh.read())
+    h.update(" ".join(NVCC_FLAGS).encode())
+    return h.hexdigest()
+
+
+def build(force=False, verbose=False):
+    os.makedirs(OUT, exist_ok=True)
+    stamp = os.path.join(OUT, "stamp")
+    dig = _digest()
+    if (not force and os.path.exists(LIB) and os.path.exists(PROBE) and os.path.exists(stamp)
+            and open(stamp).read() == dig):
+        return LIB
+    nvcc = _nvcc()
+
+    def compile_one(src):
+        obj = os.path.join(OUT, src.replace(".cu", ".o"))
+        cmd = [nvcc] + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
+        if verbose:
+            sys.stderr.write(r.stderr)
+        return obj
+
+    with ThreadPoolExecutor(len(SOURCES) + len(PROBE_SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES + PROBE_SOURCES))
+    for target, o in ((LIB, objs[:len(SOURCES)]), (PROBE, objs[len(SOURCES):])):
+        tmp = target + ".tmp"
+        cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + o
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stderr}")
+        os.replace(tmp, target)
+    with open(stamp, "w") as f:
+        f.write(dig)
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv, verbose=True))

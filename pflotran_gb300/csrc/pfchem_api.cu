@@ -1,0 +1,597 @@
+// pfchem_api.cu -- the C ABI (include/pfchem.h) over the sm_103a kernels.
+//
+// A context owns a CUDA stream, the flattened network (DevNet), the work
+// queue / statistics scratch, device staging buffers for host-pointer calls,
+// a captured CUDA graph of the last device-pointer solve, and the launch
+// mapping.  Nothing here computes chemistry on the host.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "../../include/pfchem.h"
+#include "pfchem_device.cuh"
+
+namespace pfchem {
+cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
+                         cudaStream_t st);
+cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
+int max_active_blocks(const DevNet &n, int block);
+}  // namespace pfchem
+
+using namespace pfchem;
+
+struct StageBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct pfchem_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  DevNet net;
+  bool has_net = false;
+  pfchem_options opt;
+  Scratch *scratch = nullptr;  // device
+  pfchem_launch launch{};
+  bool launch_forced = false;
+  pfchem_stats stats{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  StageBuf stage[32];
+  // graph cache of the last device-pointer solve
+  cudaGraphExec_t graph = nullptr;
+  CellArgs graph_args{};
+  pfchem_launch graph_launch{};
+  char err[512] = {0};
+};
+
+namespace {
+
+int fail(pfchem_ctx *c, int code, const char *fmt, ...) {
+  if (c) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(c->err, sizeof(c->err), fmt, ap);
+    va_end(ap);
+  }
+  return code;
+}
+
+#define CUDA_TRY(ctx, expr)                                                                     \
+  do {                                                                                          \
+    cudaError_t e_ = (expr);                                                                    \
+    if (e_ != cudaSuccess) return fail(ctx, -2, "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), \
+                                       __FILE__, __LINE__);                                     \
+  } while (0)
+
+int idtab(const int32_t *t, int ld, int k, int r) { return t[(ld + 1) * r + k]; }
+double sttab(const double *t, int ld, int k, int r) { return t[ld * r + (k - 1)]; }
+
+int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o, DevNet &n) {
+  std::memset(&n, 0, sizeof(n));
+  if (!w || !o) return fail(c, -1, "null network or options");
+  if (w->naqcomp < 1 || w->naqcomp > PFCHEM_MAX_PRI) return fail(c, -1, "naqcomp %d outside [1,%d]", w->naqcomp, PFCHEM_MAX_PRI);
+  if (w->neqcplx < 0 || w->neqcplx > PFCHEM_MAX_CPLX) return fail(c, -1, "neqcplx %d > %d", w->neqcplx, PFCHEM_MAX_CPLX);
+  if (w->nkinmnrl < 0 || w->nkinmnrl > PFCHEM_MAX_MNRL) return fail(c, -1, "nkinmnrl %d > %d", w->nkinmnrl, PFCHEM_MAX_MNRL);
+  if (w->neqionxrxn < 0 || w->neqionxrxn > PFCHEM_MAX_IONX) return fail(c, -1, "neqionxrxn %d > %d", w->neqionxrxn, PFCHEM_MAX_IONX);
+  if (w->nsrfcplxrxn < 0 || w->nsrfcplxrxn > PFCHEM_MAX_SRFRXN) return fail(c, -1, "nsrfcplxrxn %d > %d", w->nsrfcplxrxn, PFCHEM_MAX_SRFRXN);
+  if (w->nsrfcplx < 0 || w->nsrfcplx > PFCHEM_MAX_SRFCPLX) return fail(c, -1, "nsrfcplx %d > %d", w->nsrfcplx, PFCHEM_MAX_SRFCPLX);
+  if (w->max_num_prefactors > 0 && w->kinmnrl_num_prefactors) {
+    for (int m = 0; m < w->nkinmnrl; ++m)
+      if (w->kinmnrl_num_prefactors[m] > 0) return fail(c, -1, "mineral %d: rate prefactors are not supported by the device kernels", m + 1);
+  }
+  if (o->act_coef_update_algorithm == PFCHEM_ACT_COEF_ALGORITHM_NEWTON && o->act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF)
+    return fail(c, -1, "ACT_COEF_ALGORITHM_NEWTON is not supported by the device kernels (use LAG)");
+  if (o->use_activity_h2o && o->act_coef_update_frequency == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER)
+    return fail(c, -1, "use_activity_h2o with NEWTON_ITER activity updates is not supported");
+  if (o->max_iterations < 1) return fail(c, -1, "max_iterations must be >= 1");
+  n.N = w->naqcomp;
+  n.Nc = w->neqcplx;
+  n.Nm = w->nkinmnrl;
+  n.Nix = w->neqionxrxn;
+  n.Nsr = w->nsrfcplxrxn;
+  n.Nsc = w->nsrfcplx;
+  n.use_log = o->use_log_formulation != 0;
+  n.act_freq = o->act_coef_update_frequency;
+  n.use_h2o = o->use_activity_h2o != 0;
+  n.isothermal = o->use_isothermal != 0;
+  n.resid_kind = o->residual_tol_kind;
+  n.accum_mode = o->accum_mode;
+  n.max_iter = o->max_iterations;
+  n.update_kin = o->update_kinetic_state != 0;
+  n.max_dlnC = o->max_dlnC;
+  n.rel_change_tol = o->max_relative_change_tolerance;
+  n.res_tol = o->max_residual_tolerance;
+  n.A = w->debyeA;
+  n.B = w->debyeB;
+  n.Bdot = w->debyeBdot;
+  for (int j = 0; j < n.N; ++j) {
+    n.Zp[j] = w->primary_spec_Z[j];
+    n.Z2p[j] = std::fabs(n.Zp[j]) > 1e-10 ? n.Zp[j] * n.Zp[j] : 0.0;
+    n.ap[j] = w->primary_spec_a0[j];
+  }
+  auto check_ids = [&](const char *what, const int32_t *t, int ld, int cnt, int maxid) -> int {
+    if (cnt > 0 && !t) return fail(c, -1, "%s: table missing", what);
+    if (ld > PFCHEM_MAX_NNZ) return fail(c, -1, "%s: leading dimension %d > %d", what, ld, PFCHEM_MAX_NNZ);
+    for (int r = 0; r < cnt; ++r) {
+      int k = idtab(t, ld, 0, r);
+      if (k < 0 || k > ld) return fail(c, -1, "%s %d: count %d outside [0,%d]", what, r + 1, k, ld);
+      for (int q = 1; q <= k; ++q) {
+        int id = idtab(t, ld, q, r);
+        if (id < 1 || id > maxid) return fail(c, -1, "%s %d: species id %d outside [1,%d]", what, r + 1, id, maxid);
+      }
+    }
+    return 0;
+  };
+  int e;
+  if ((e = check_ids("aqueous complex", w->eqcplxspecid, w->eqcplx_ld, n.Nc, n.N))) return e;
+  for (int i = 0; i < n.Nc; ++i) {
+    n.cn[i] = (int8_t)idtab(w->eqcplxspecid, w->eqcplx_ld, 0, i);
+    for (int k = 1; k <= n.cn[i]; ++k) {
+      n.cid[i][k - 1] = (int8_t)(idtab(w->eqcplxspecid, w->eqcplx_ld, k, i) - 1);
+      n.cnu[i][k - 1] = sttab(w->eqcplxstoich, w->eqcplx_ld, k, i);
+    }
+    n.cZ2[i] = std::fabs(w->eqcplx_Z[i]) > 1e-10 ? w->eqcplx_Z[i] * w->eqcplx_Z[i] : 0.0;
+    n.ca[i] = w->eqcplx_a0[i];
+    n.ch2o[i] = (w->eqcplxh2oid && w->eqcplxh2oid[i] > 0) ? w->eqcplxh2ostoich[i] : 0.0;
+    n.clogK[i] = w->eqcplx_logK ? w->eqcplx_logK[i] : 0.0;
+    for (int q = 0; q < 5; ++q) n.ccoef[i][q] = w->eqcplx_logKcoef ? w->eqcplx_logKcoef[5 * i + q] : 0.0;
+  }
+  if ((e = check_ids("kinetic mineral", w->kinmnrlspecid, w->kinmnrl_ld, n.Nm, n.N))) return e;
+  n.has_temkin = w->kinmnrl_Temkin_const != nullptr;
+  n.has_minscale = w->kinmnrl_min_scale_factor != nullptr;
+  n.has_affpow = w->kinmnrl_affinity_power != nullptr;
+  for (int m = 0; m < n.Nm; ++m) {
+    n.mn[m] = (int8_t)idtab(w->kinmnrlspecid, w->kinmnrl_ld, 0, m);
+    for (int k = 1; k <= n.mn[m]; ++k) {
+      n.mid[m][k - 1] = (int8_t)(idtab(w->kinmnrlspecid, w->kinmnrl_ld, k, m) - 1);
+      n.mnu[m][k - 1] = sttab(w->kinmnrlstoich, w->kinmnrl_ld, k, m);
+    }
+    n.mh2o[m] = (w->kinmnrlh2oid && w->kinmnrlh2oid[m] > 0) ? w->kinmnrlh2ostoich[m] : 0.0;
+    n.mlogK[m] = w->kinmnrl_logK ? w->kinmnrl_logK[m] : 0.0;
+    for (int q = 0; q < 5; ++q) n.mcoef[m][q] = w->kinmnrl_logKcoef ? w->kinmnrl_logKcoef[5 * m + q] : 0.0;
+    n.mk[m] = w->kinmnrl_rate_constant[m];
+    n.mEa[m] = w->kinmnrl_activation_energy ? w->kinmnrl_activation_energy[m] : 0.0;
+    n.mVm[m] = w->kinmnrl_molar_vol[m];
+    n.mthr[m] = w->kinmnrl_affinity_threshold ? w->kinmnrl_affinity_threshold[m] : 0.0;
+    n.mlim[m] = w->kinmnrl_rate_limiter ? w->kinmnrl_rate_limiter[m] : 0.0;
+    n.mtemkin[m] = n.has_temkin ? w->kinmnrl_Temkin_const[m] : 1.0;
+    n.mscale[m] = n.has_minscale ? w->kinmnrl_min_scale_factor[m] : 1.0;
+    n.mpow[m] = n.has_affpow ? w->kinmnrl_affinity_power[m] : 1.0;
+  }
+  if ((e = check_ids("ion exchange", w->eqionx_rxn_cationid, w->eqionx_ld, n.Nix, n.N))) return e;
+  for (int r = 0; r < n.Nix; ++r) {
+    n.xn[r] = (int8_t)idtab(w->eqionx_rxn_cationid, w->eqionx_ld, 0, r);
+    if (n.xn[r] < 1) return fail(c, -1, "ion exchange %d has no cations", r + 1);
+    n.xzflag[r] = w->eqionx_rxn_Z_flag[r] ? 1 : 0;
+    n.xsurf[r] = (int8_t)(w->eqionx_rxn_to_surf ? w->eqionx_rxn_to_surf[r] : 0);
+    if (n.xsurf[r] < 0 || n.xsurf[r] > n.Nm) return fail(c, -1, "ion exchange %d: mineral id %d", r + 1, n.xsurf[r]);
+    n.xCEC[r] = w->eqionx_rxn_CEC[r];
+    const int i1 = idtab(w->eqionx_rxn_cationid, w->eqionx_ld, 1, r) - 1;
+    for (int k = 1; k <= n.xn[r]; ++k) {
+      const int id = idtab(w->eqionx_rxn_cationid, w->eqionx_ld, k, r) - 1;
+      n.xid[r][k - 1] = (int8_t)id;
+      n.xk[r][k - 1] = sttab(w->eqionx_rxn_k, w->eqionx_ld, k, r);
+      if (std::fabs(n.Zp[id]) < 1e-10) return fail(c, -1, "ion exchange %d: uncharged cation", r + 1);
+      const double zr = n.Zp[id] / n.Zp[i1];
+      n.xzr[r][k - 1] = zr;
+      n.xpow[r][k - 1] = zr == 1.0 ? kPowOne : zr == 2.0 ? kPowTwo : zr == 0.5 ? kPowHalf : kPowGeneric;
+    }
+  }
+  if ((e = check_ids("surface complex", w->srfcplxspecid, w->srfcplx_ld, n.Nsc, n.N))) return e;
+  if ((e = check_ids("surface complexation reaction", w->srfcplxrxn_to_complex, w->srfcplxrxn_ld, n.Nsr, n.Nsc)))
+    return e;
+  for (int r = 0; r < n.Nsr; ++r) {
+    n.srn[r] = (int8_t)idtab(w->srfcplxrxn_to_complex, w->srfcplxrxn_ld, 0, r);
+    for (int k = 1; k <= n.srn[r]; ++k) n.src[r][k - 1] = (int8_t)(idtab(w->srfcplxrxn_to_complex, w->srfcplxrxn_ld, k, r) - 1);
+    n.srtype[r] = (int8_t)w->srfcplxrxn_surf_type[r];
+    if (n.srtype[r] == PFCHEM_COLLOID_SURFACE) return fail(c, -1, "surface complexation %d: colloid surfaces are not supported", r + 1);
+    n.srsurf[r] = (int8_t)(w->srfcplxrxn_to_surf ? w->srfcplxrxn_to_surf[r] : 0);
+    if (n.srtype[r] == PFCHEM_MINERAL_SURFACE && (n.srsurf[r] < 1 || n.srsurf[r] > n.Nm))
+      return fail(c, -1, "surface complexation %d: mineral id %d", r + 1, n.srsurf[r]);
+    n.srdens[r] = w->srfcplxrxn_site_density[r];
+    n.srflag[r] = w->srfcplxrxn_stoich_flag[r] ? 1 : 0;
+  }
+  for (int k = 0; k < n.Nsc; ++k) {
+    n.sn[k] = (int8_t)idtab(w->srfcplxspecid, w->srfcplx_ld, 0, k);
+    for (int q = 1; q <= n.sn[k]; ++q) {
+      n.sid[k][q - 1] = (int8_t)(idtab(w->srfcplxspecid, w->srfcplx_ld, q, k) - 1);
+      n.snu[k][q - 1] = sttab(w->srfcplxstoich, w->srfcplx_ld, q, k);
+    }
+    n.sfs[k] = w->srfcplx_free_site_stoich[k];
+    n.sh2o[k] = (w->srfcplxh2oid && w->srfcplxh2oid[k] > 0) ? w->srfcplxh2ostoich[k] : 0.0;
+    n.slogK[k] = w->srfcplx_logK ? w->srfcplx_logK[k] : 0.0;
+    for (int q = 0; q < 5; ++q) n.scoef[k][q] = w->srfcplx_logKcoef ? w->srfcplx_logKcoef[5 * k + q] : 0.0;
+  }
+  return 0;
+}
+
+int stage(pfchem_ctx *c, int slot, const void *host, size_t bytes, void **dev, bool upload) {
+  *dev = nullptr;
+  if (!host) return 0;
+  StageBuf &b = c->stage[slot];
+  if (b.bytes < bytes) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    CUDA_TRY(c, cudaMalloc(&b.ptr, bytes));
+    b.bytes = bytes;
+  }
+  if (upload) CUDA_TRY(c, cudaMemcpyAsync(b.ptr, host, bytes, cudaMemcpyHostToDevice, c->stream));
+  *dev = b.ptr;
+  return 0;
+}
+
+// Default mapping: 64 threads per block, as many resident blocks per SM as
+// fit, refill when 8 lanes of a warp are idle.
+void default_launch(pfchem_ctx *c) {
+  c->launch.block_threads = 64;
+  int nb = max_active_blocks(c->net, 64);
+  c->launch.blocks_per_sm = std::max(1, nb);
+  c->launch.refill_min_idle = 8;
+}
+
+int check_cells(pfchem_ctx *c, const pfchem_cells *cl) {
+  if (!c || !cl) return fail(c, -1, "null argument");
+  if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
+  if (cl->ncells < 0) return fail(c, -1, "ncells < 0");
+  const DevNet &n = c->net;
+  if (!cl->temperature || !cl->saturation || !cl->den_kg || !cl->porosity || !cl->volume || !cl->pri_molal ||
+      !cl->ionic_strength)
+    return fail(c, -1, "a required per-cell array is null");
+  if (n.Nm > 0 && (!cl->mnrl_volfrac || !cl->mnrl_area)) return fail(c, -1, "mnrl_volfrac/mnrl_area required");
+  if (n.Nix + n.Nsr > 0 && !cl->total_sorb_eq) return fail(c, -1, "total_sorb_eq required with sorption");
+  if (n.Nix > 0 && !cl->eqionx_ref_cation_sorbed_conc) return fail(c, -1, "eqionx_ref_cation_sorbed_conc required");
+  if (n.Nsr > 0 && !cl->srfcplxrxn_free_site_conc) return fail(c, -1, "srfcplxrxn_free_site_conc required");
+  bool rock = false;
+  for (int r = 0; r < n.Nsr; ++r) rock |= n.srtype[r] == PFCHEM_ROCK_SURFACE;
+  if (rock && !cl->soil_particle_density) return fail(c, -1, "soil_particle_density required for ROCK surfaces");
+  if (n.use_h2o && !cl->ln_act_h2o) return fail(c, -1, "ln_act_h2o required with use_activity_h2o");
+  return 0;
+}
+
+// Fills CellArgs from a pfchem_cells whose pointers are device pointers.
+CellArgs device_args(const pfchem_cells *cl, double dt) {
+  CellArgs a{};
+  a.ncells = cl->ncells;
+  a.dt = dt;
+  a.temp = cl->temperature;
+  a.sat = cl->saturation;
+  a.den = cl->den_kg;
+  a.por = cl->porosity;
+  a.vol = cl->volume;
+  a.rho_s = cl->soil_particle_density;
+  a.active = cl->active;
+  a.total = cl->total;
+  a.total_stride_cell = 1;
+  a.total_stride_comp = cl->ncells;
+  a.pri_molal = cl->pri_molal;
+  a.ionic = cl->ionic_strength;
+  a.lnaw = cl->ln_act_h2o;
+  a.vf = cl->mnrl_volfrac;
+  a.area = cl->mnrl_area;
+  a.sorb = cl->total_sorb_eq;
+  a.ixref = cl->eqionx_ref_cation_sorbed_conc;
+  a.srfree = cl->srfcplxrxn_free_site_conc;
+  a.total_out = cl->total_out;
+  a.rate = cl->mnrl_rate;
+  a.sec_molal = cl->sec_molal;
+  a.iters = cl->iterations;
+  a.status = cl->status;
+  a.alt_guess = cl->alt_guess;
+  a.interleaved_out = nullptr;
+  return a;
+}
+
+int run_solve(pfchem_ctx *c, const CellArgs &a) {
+  const DevNet &n = c->net;
+  if (a.ncells == 0) {
+    c->stats = pfchem_stats{};
+    return 0;
+  }
+  const pfchem_launch &L = c->launch;
+  const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
+  const bool same = c->graph && std::memcmp(&a, &c->graph_args, sizeof(CellArgs)) == 0 &&
+                    std::memcmp(&L, &c->graph_launch, sizeof(pfchem_launch)) == 0;
+  if (!same) {
+    // capture memset(scratch) + solve into a graph and keep it for replays
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+    cudaGraph_t g;
+    CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream);
+    cudaError_t le = launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
+    cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
+    if (ce != cudaSuccess) return fail(c, -2, "graph capture: %s", cudaGetErrorString(ce));
+    cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) return fail(c, -2, "graph instantiate: %s", cudaGetErrorString(ie));
+    c->graph_args = a;
+    c->graph_launch = L;
+  }
+  CUDA_TRY(c, cudaEventRecord(c->ev0, c->stream));
+  CUDA_TRY(c, cudaGraphLaunch(c->graph, c->stream));
+  CUDA_TRY(c, cudaEventRecord(c->ev1, c->stream));
+  Scratch h;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->scratch, sizeof(Scratch), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+  c->stats.ncells = a.ncells;
+  c->stats.sum_iterations = (int64_t)h.sum_iter;
+  c->stats.max_iterations = (int32_t)h.max_iter;
+  c->stats.nonconverged = (int32_t)h.nonconverged;
+  c->stats.alt_guess_used = (int64_t)h.alt_used;
+  c->stats.kernel_ms = ms;
+  return (int)h.nonconverged;
+}
+
+int react_host(pfchem_ctx *c, double dt, pfchem_cells *cl, double *tran_xx, int32_t ncomp) {
+  const DevNet &n = c->net;
+  const int64_t nc = cl->ncells;
+  const size_t d1 = nc * sizeof(double), dN = n.N * d1, dM = std::max(n.Nm, 1) * d1;
+  CellArgs a{};
+  void *p;
+  int e = 0;
+#define ST(slot, ptr, bytes, up)                                 \
+  if ((e = stage(c, slot, (ptr), (bytes), &p, (up))) != 0) return e; \
+  (void)0
+  ST(0, cl->temperature, d1, true); a.temp = (const double *)p;
+  ST(1, cl->saturation, d1, true); a.sat = (const double *)p;
+  ST(2, cl->den_kg, d1, true); a.den = (const double *)p;
+  ST(3, cl->porosity, d1, true); a.por = (const double *)p;
+  ST(4, cl->volume, d1, true); a.vol = (const double *)p;
+  ST(5, cl->soil_particle_density, d1, true); a.rho_s = (const double *)p;
+  ST(6, cl->active, nc * sizeof(int32_t), true); a.active = (const int32_t *)p;
+  if (tran_xx) {
+    ST(7, tran_xx, (size_t)ncomp * d1, true);
+    a.total = (const double *)p;
+    a.interleaved_out = (double *)p;
+    a.total_stride_cell = ncomp;
+    a.total_stride_comp = 1;
+  } else {
+    ST(7, cl->total, dN, true);
+    a.total = (const double *)p;
+    a.total_stride_cell = 1;
+    a.total_stride_comp = nc;
+  }
+  ST(8, cl->pri_molal, dN, true); a.pri_molal = (double *)p;
+  ST(9, cl->ionic_strength, d1, true); a.ionic = (double *)p;
+  ST(10, cl->ln_act_h2o, d1, true); a.lnaw = (double *)p;
+  ST(11, cl->mnrl_volfrac, dM, true); a.vf = (double *)p;
+  ST(12, cl->mnrl_area, dM, true); a.area = (double *)p;
+  ST(13, cl->total_sorb_eq, dN, true); a.sorb = (double *)p;
+  ST(14, cl->eqionx_ref_cation_sorbed_conc, std::max(n.Nix, 1) * d1, true); a.ixref = (double *)p;
+  ST(15, cl->srfcplxrxn_free_site_conc, std::max(n.Nsr, 1) * d1, true); a.srfree = (double *)p;
+  ST(16, cl->total_out, dN, false); a.total_out = (double *)p;
+  ST(17, cl->mnrl_rate, dM, false); a.rate = (double *)p;
+  ST(18, cl->sec_molal, std::max(n.Nc, 1) * d1, false); a.sec_molal = (double *)p;
+  ST(19, cl->iterations, nc * sizeof(int32_t), false); a.iters = (int32_t *)p;
+  ST(20, cl->status, nc * sizeof(int32_t), false); a.status = (int32_t *)p;
+  ST(21, cl->alt_guess, dN, true); a.alt_guess = (const double *)p;
+#undef ST
+  a.ncells = nc;
+  a.dt = dt;
+  int r = run_solve(c, a);
+  if (r < 0) return r;
+  auto down = [&](void *host, const void *dev, size_t bytes) -> int {
+    if (host && dev) CUDA_TRY(c, cudaMemcpyAsync(host, dev, bytes, cudaMemcpyDeviceToHost, c->stream));
+    return 0;
+  };
+  if ((e = down(cl->pri_molal, a.pri_molal, dN))) return e;
+  if ((e = down(cl->ionic_strength, a.ionic, d1))) return e;
+  if ((e = down(cl->ln_act_h2o, a.lnaw, d1))) return e;
+  if ((e = down(cl->mnrl_volfrac, a.vf, dM))) return e;
+  if ((e = down(cl->total_sorb_eq, a.sorb, dN))) return e;
+  if ((e = down(cl->eqionx_ref_cation_sorbed_conc, a.ixref, std::max(n.Nix, 1) * d1))) return e;
+  if ((e = down(cl->srfcplxrxn_free_site_conc, a.srfree, std::max(n.Nsr, 1) * d1))) return e;
+  if ((e = down(cl->total_out, a.total_out, dN))) return e;
+  if ((e = down(cl->mnrl_rate, a.rate, dM))) return e;
+  if ((e = down(cl->sec_molal, a.sec_molal, std::max(n.Nc, 1) * d1))) return e;
+  if ((e = down(cl->iterations, a.iters, nc * sizeof(int32_t)))) return e;
+  if ((e = down(cl->status, a.status, nc * sizeof(int32_t)))) return e;
+  if (tran_xx && (e = down(tran_xx, a.total, (size_t)ncomp * d1))) return e;
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return r;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pfchem_create(pfchem_ctx **out, int device) {
+  if (!out) return -1;
+  *out = nullptr;
+  pfchem_ctx *c = new pfchem_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    delete c;
+    return -2;
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaMalloc(&c->scratch, sizeof(Scratch)) != cudaSuccess || cudaEventCreate(&c->ev0) != cudaSuccess ||
+      cudaEventCreate(&c->ev1) != cudaSuccess) {
+    pfchem_destroy(c);
+    return -2;
+  }
+  *out = c;
+  return 0;
+}
+
+void pfchem_destroy(pfchem_ctx *c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  for (auto &b : c->stage)
+    if (b.ptr) cudaFree(b.ptr);
+  if (c->scratch) cudaFree(c->scratch);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char *pfchem_last_error(const pfchem_ctx *c) { return c ? c->err : "null context"; }
+
+int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_options *opt) {
+  if (!c) return -1;
+  cudaSetDevice(c->device);
+  DevNet n;
+  int e = build_devnet(c, net, opt, n);
+  if (e) return e;
+  c->net = n;
+  c->opt = *opt;
+  c->has_net = true;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  if (!c->launch_forced) default_launch(c);
+  return 0;
+}
+
+int pfchem_react_batch(pfchem_ctx *c, double dt, pfchem_cells *cl) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  if (!cl->total) return fail(c, -1, "total is null");
+  cudaSetDevice(c->device);
+  if (cl->on_device) return run_solve(c, device_args(cl, dt));
+  return react_host(c, dt, cl, nullptr, 0);
+}
+
+int pfchem_react_batch_interleaved(pfchem_ctx *c, double dt, int32_t ncomp, double *tran_xx, pfchem_cells *cl) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!tran_xx) return fail(c, -1, "tran_xx is null");
+  if (ncomp < c->net.N) return fail(c, -1, "ncomp %d < naqcomp %d", ncomp, c->net.N);
+  if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  cudaSetDevice(c->device);
+  if (cl->on_device) {
+    CellArgs a = device_args(cl, dt);
+    a.total = tran_xx;
+    a.interleaved_out = tran_xx;
+    a.total_stride_cell = ncomp;
+    a.total_stride_comp = 1;
+    return run_solve(c, a);
+  }
+  return react_host(c, dt, cl, tran_xx, ncomp);
+}
+
+int pfchem_update_kinetic_state(pfchem_ctx *c, double dt, pfchem_cells *cl) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device) return fail(c, -1, "pfchem_update_kinetic_state takes device pointers");
+  if (!cl->total) return fail(c, -1, "total is null");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, dt);
+  if (a.ncells == 0) return 0;
+  cudaError_t le = launch_kinetic_state(c->net, a, c->stream);
+  if (le != cudaSuccess) return fail(c, -2, "kinetic-state launch: %s", cudaGetErrorString(le));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int pfchem_last_stats(const pfchem_ctx *c, pfchem_stats *s) {
+  if (!c || !s) return -1;
+  *s = c->stats;
+  return 0;
+}
+
+int pfchem_get_launch(const pfchem_ctx *c, pfchem_launch *l) {
+  if (!c || !l) return -1;
+  *l = c->launch;
+  return 0;
+}
+
+int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
+  if (!c || !l) return -1;
+  if (l->block_threads < 32 || l->block_threads > 256 || l->block_threads % 32)
+    return fail(c, -1, "block_threads must be a multiple of 32 in [32, 256]");
+  if (l->refill_min_idle < 1 || l->refill_min_idle > 32) return fail(c, -1, "refill_min_idle must be in [1, 32]");
+  if (l->blocks_per_sm < 1) return fail(c, -1, "blocks_per_sm must be >= 1");
+  if (c->has_net) {
+    const size_t shm = (size_t)c->net.N * c->net.N * l->block_threads * sizeof(double);
+    if (shm > 227 * 1024) return fail(c, -1, "block_threads %d needs %zu bytes of shared memory", l->block_threads, shm);
+    int nb = max_active_blocks(c->net, l->block_threads);
+    if (nb < 1) return fail(c, -1, "mapping does not fit on an SM");
+  }
+  c->launch = *l;
+  c->launch_forced = true;
+  return 0;
+}
+
+int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device) return fail(c, -1, "pfchem_autotune takes device pointers");
+  cudaSetDevice(c->device);
+  const DevNet &n = c->net;
+  const int64_t nc = cl->ncells;
+  // back up every array a solve writes, restore after each trial
+  struct Arr {
+    double *p;
+    size_t bytes;
+    void *save;
+  };
+  std::vector<Arr> arrs;
+  auto add = [&](double *p, size_t k) {
+    if (p) arrs.push_back({p, k * nc * sizeof(double), nullptr});
+  };
+  add(cl->pri_molal, n.N);
+  add(cl->ionic_strength, 1);
+  add(cl->ln_act_h2o, 1);
+  add(cl->mnrl_volfrac, std::max(n.Nm, 1));
+  add(cl->total_sorb_eq, n.N);
+  add(cl->eqionx_ref_cation_sorbed_conc, std::max(n.Nix, 1));
+  add(cl->srfcplxrxn_free_site_conc, std::max(n.Nsr, 1));
+  for (auto &x : arrs) {
+    CUDA_TRY(c, cudaMalloc(&x.save, x.bytes));
+    CUDA_TRY(c, cudaMemcpyAsync(x.save, x.p, x.bytes, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  const int blocks[] = {32, 64, 128};
+  const int refills[] = {1, 8, 16, 32};
+  double best = 1e30;
+  pfchem_launch best_l = c->launch;
+  int rc = 0;
+  for (int b : blocks) {
+    const size_t shm = (size_t)n.N * n.N * b * sizeof(double);
+    if (shm > 227 * 1024) continue;
+    int nb = max_active_blocks(n, b);
+    if (nb < 1) continue;
+    for (int r : refills) {
+      pfchem_launch l{b, nb, r, 0};
+      c->launch = l;
+      rc = pfchem_react_batch(c, dt, cl);
+      if (rc < 0) break;
+      const double ms = c->stats.kernel_ms;
+      if (ms < best) {
+        best = ms;
+        best_l = l;
+      }
+      for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+    }
+    if (rc < 0) break;
+  }
+  for (auto &x : arrs) {
+    cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+  }
+  cudaStreamSynchronize(c->stream);
+  for (auto &x : arrs) cudaFree(x.save);
+  if (rc < 0) return rc;
+  c->launch = best_l;
+  c->launch_forced = true;
+  return 0;
+}
+
+}  // extern "C"

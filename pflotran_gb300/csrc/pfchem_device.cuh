@@ -1,0 +1,94 @@
+// pfchem_device.cuh -- device-side network description and kernel arguments.
+//
+// The host (pfchem_api.cu) flattens a pfchem_network into a DevNet: 0-based
+// species ids, stoichiometry with pre-computed |nu|, squared charges, and the
+// per-reaction constants the Newton kernel needs.  A DevNet is passed to the
+// kernels by value as a __grid_constant__ parameter, so it lives in the
+// constant bank (uniform reads broadcast across a warp) and every context
+// keeps its own network without global device state.
+#pragma once
+#include <stdint.h>
+
+#include "../../include/pfchem.h"
+
+namespace pfchem {
+
+constexpr double kLOG_TO_LN = 2.30258509299;    // pflotran_constants.F90:48
+constexpr double kIDEAL_GAS_CONSTANT = 8.31446;  // pflotran_constants.F90:53
+
+// Power kinds of KDj^(Z_j / Z_ref) in the ion-exchange inner Newton.
+enum : int8_t { kPowOne = 0, kPowTwo = 1, kPowHalf = 2, kPowGeneric = 3 };
+
+struct DevNet {
+  int32_t N, Nc, Nm, Nix, Nsr, Nsc;
+  // options
+  int32_t use_log, act_freq, use_h2o, isothermal, resid_kind, accum_mode, max_iter, update_kin;
+  int32_t has_temkin, has_minscale, has_affpow, has_h2o_rxn;
+  double max_dlnC, rel_change_tol, res_tol;
+  double A, B, Bdot;
+  // primaries
+  double Z2p[PFCHEM_MAX_PRI], ap[PFCHEM_MAX_PRI], Zp[PFCHEM_MAX_PRI];
+  // aqueous complexes
+  int8_t cn[PFCHEM_MAX_CPLX];
+  int8_t cid[PFCHEM_MAX_CPLX][PFCHEM_MAX_NNZ];
+  double cnu[PFCHEM_MAX_CPLX][PFCHEM_MAX_NNZ];
+  double cZ2[PFCHEM_MAX_CPLX], ca[PFCHEM_MAX_CPLX], ch2o[PFCHEM_MAX_CPLX];
+  double clogK[PFCHEM_MAX_CPLX];
+  double ccoef[PFCHEM_MAX_CPLX][5];
+  // kinetic minerals
+  int8_t mn[PFCHEM_MAX_MNRL];
+  int8_t mid[PFCHEM_MAX_MNRL][PFCHEM_MAX_NNZ];
+  double mnu[PFCHEM_MAX_MNRL][PFCHEM_MAX_NNZ];
+  double mh2o[PFCHEM_MAX_MNRL], mlogK[PFCHEM_MAX_MNRL], mcoef[PFCHEM_MAX_MNRL][5];
+  double mk[PFCHEM_MAX_MNRL], mEa[PFCHEM_MAX_MNRL], mVm[PFCHEM_MAX_MNRL];
+  double mthr[PFCHEM_MAX_MNRL], mlim[PFCHEM_MAX_MNRL];
+  double mtemkin[PFCHEM_MAX_MNRL], mscale[PFCHEM_MAX_MNRL], mpow[PFCHEM_MAX_MNRL];
+  // ion exchange
+  int8_t xn[PFCHEM_MAX_IONX], xzflag[PFCHEM_MAX_IONX], xsurf[PFCHEM_MAX_IONX];
+  int8_t xid[PFCHEM_MAX_IONX][PFCHEM_MAX_NNZ];
+  int8_t xpow[PFCHEM_MAX_IONX][PFCHEM_MAX_NNZ];
+  double xk[PFCHEM_MAX_IONX][PFCHEM_MAX_NNZ];
+  double xzr[PFCHEM_MAX_IONX][PFCHEM_MAX_NNZ];  // Z_j / Z_ref
+  double xCEC[PFCHEM_MAX_IONX];
+  // surface complexation (reactions, then their complexes)
+  int8_t srn[PFCHEM_MAX_SRFRXN], srtype[PFCHEM_MAX_SRFRXN], srsurf[PFCHEM_MAX_SRFRXN], srflag[PFCHEM_MAX_SRFRXN];
+  int8_t src[PFCHEM_MAX_SRFRXN][PFCHEM_MAX_NNZ];
+  double srdens[PFCHEM_MAX_SRFRXN];
+  int8_t sn[PFCHEM_MAX_SRFCPLX];
+  int8_t sid[PFCHEM_MAX_SRFCPLX][PFCHEM_MAX_NNZ];
+  double snu[PFCHEM_MAX_SRFCPLX][PFCHEM_MAX_NNZ];
+  double sfs[PFCHEM_MAX_SRFCPLX], sh2o[PFCHEM_MAX_SRFCPLX], slogK[PFCHEM_MAX_SRFCPLX];
+  double scoef[PFCHEM_MAX_SRFCPLX][5];
+};
+
+// Per-call pointers (device memory, SoA, field(i, cell) at [i * ncells + cell]).
+struct CellArgs {
+  int64_t ncells;
+  double dt;
+  const double *temp, *sat, *den, *por, *vol, *rho_s;
+  const int32_t *active;
+  const double *total;
+  int64_t total_stride_cell;  // 1 for SoA; ncomp for RTReact's interleaved tran_xx
+  int64_t total_stride_comp;  // ncells for SoA; 1 for interleaved
+  double *pri_molal, *ionic, *lnaw, *vf, *area, *sorb, *ixref, *srfree;
+  double *total_out, *rate, *sec_molal;
+  int32_t *iters, *status;
+  const double *alt_guess;
+  double *interleaved_out;  // RTReact layout write-back of the free ions, or null
+};
+
+// Work queue and statistics: global memory the solve kernel uses besides its
+// inputs and outputs.
+struct Scratch {
+  unsigned long long next_cell;  // work-queue head
+  unsigned long long sum_iter;
+  unsigned long long alt_used;
+  unsigned int max_iter;
+  unsigned int nonconverged;
+};
+
+struct LaunchCfg {
+  int refill_min_idle;
+};
+
+}  // namespace pfchem

@@ -75,27 +75,35 @@ def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rh
     # charges: >= 4 cations (Z > 0) for ion exchange, the rest in {-2..2}
     Z = np.array([1, 2, 1, 2, 1, -1, -2, -1, 0, 1, -1, 2], dtype=float)[:N]
     rng.shuffle(Z)
+    # species 0 plays the part of H+: the only species with negative
+    # coefficients (deprotonation reactions), so only its total can be < 0
+    Z[[0, int(np.flatnonzero(Z == 1)[0])]] = Z[[int(np.flatnonzero(Z == 1)[0]), 0]]
     a0 = rng.uniform(3.0, 9.0, N)
     names = [f"P{i}" for i in range(N)]
     net = ReactionNetwork([(names[i], Z[i], a0[i]) for i in range(N)])
     lm_ref = np.log(1e-5)
 
-    def draw_rxn(nnz_choices=(2, 3, 3, 4), lo=-14.0, hi=-3.0, force_pos=True):
-        while True:
+    def draw_rxn(nnz_choices=(2, 3, 3, 4), lo=-14.0, hi=-3.0, force_pos=True, max_charge=None):
+        for _ in range(100000):
             nnz = int(rng.choice(nnz_choices))
             sp = rng.choice(N, nnz, replace=False)
-            nu = rng.choice([-2, -1, 1, 2], nnz, p=[0.15, 0.2, 0.45, 0.2]).astype(float)
+            nu = rng.choice([1, 2], nnz, p=[0.65, 0.35]).astype(float)
+            if 0 in sp and rng.random() < 0.5:
+                nu[list(sp).index(0)] *= -1.0
             if force_pos and nu.max() <= 0:
                 continue
+            if max_charge is not None and abs(float(nu @ Z[sp])) > max_charge:
+                continue  # complexes carry charges in {-2..2}
             logK = rng.uniform(-15.0, 15.0)
             # keep reactions whose species concentration at the reference
             # state (all free ions 1e-5 mol/kg) lies in [10^lo, 10^hi]
             log10C = -logK + nu.sum() * lm_ref / LOG_TO_LN
             if lo <= log10C <= hi:
                 return sp, nu, logK
+        raise RuntimeError("synthetic_network: no admissible reaction drawn")
 
     for i in range(Nc):
-        sp, nu, logK = draw_rxn()
+        sp, nu, logK = draw_rxn(lo=-12.0, hi=-6.0, max_charge=2.0)
         net.add_complex(f"C{i}", {names[s]: v for s, v in zip(sp, nu)}, logK, a0=rng.uniform(3.0, 9.0))
     for m in range(Nm):
         sp, nu, logK = draw_rxn(nnz_choices=(2, 3, 3, 4), lo=-2.0, hi=2.0)
@@ -106,16 +114,22 @@ def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rh
     # CEC 5 meq/100 g = 0.05 eq/kg solid -> eq/m^3 bulk (reaction.F90:657-660)
     CEC = 0.05 * rho_s * (1.0 - porosity)
     for r in range(Nix):
-        sp = rng.choice(cations, 3, replace=False)
+        sp = list(rng.choice(cations, 3, replace=False))
+        # the reference cation (first) has the smallest charge, as in
+        # PFLOTRAN's decks (Na+ reference): KDj^(Z_j/Z_ref) then has
+        # exponents >= 1 and the KDj Newton is monotone
+        sp.sort(key=lambda s: Z[s])
         ks = [1.0] + list(10.0 ** rng.uniform(-1.0, 1.0, 2))
         net.add_ion_exchange([(names[s], k) for s, k in zip(sp, ks)], CEC)
     for r in range(Nsr):
         cx = []
         for j in range(3):
-            nnz = int(rng.choice([1, 2]))
-            sp = rng.choice(N, nnz, replace=False)
-            nu = rng.choice([-1, 1, 2], nnz, p=[0.3, 0.5, 0.2]).astype(float)
             while True:
+                nnz = int(rng.choice([1, 2]))
+                sp = rng.choice(N, nnz, replace=False)
+                nu = rng.choice([1, 2], nnz, p=[0.7, 0.3]).astype(float)
+                if 0 in sp and rng.random() < 0.5:
+                    nu[list(sp).index(0)] *= -1.0
                 logK = rng.uniform(-15.0, 15.0)
                 # surface complex / free site ratio at the reference state in [1e-3, 1e1]
                 lr = -logK + nu.sum() * lm_ref / LOG_TO_LN
@@ -315,8 +329,27 @@ def calcite_cells(n=100, seed=0, temperature_dependent=False, net=None):
     return net, opt, b, dt
 
 
-def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-3, 3.0), tot_range=(1e-10, 1e-1)):
-    """Cells of the synthetic 12-species workload.  Returns (net, opt, cells, dt)."""
+def _forward_state(sp, lnm, iters=12):
+    """Totals (mol/L), complexes and the self-consistent ionic strength at free ions exp(lnm)."""
+    n = lnm.shape[0]
+    I = np.full(n, 1e-3)
+    with np.errstate(all="ignore"):
+        for _ in range(iters):
+            lngp, lngc = sp.ln_gamma(np.clip(I, 0.0, 10.0))
+            Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
+            I = sp.ionic_strength(lnm, Cc)
+    return Psi * DEN_KG_25C * 1e-3, Cc, I, lngp
+
+
+def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-2, 2.0), tot_range=(1e-10, 1e-1)):
+    """Cells of the synthetic 12-species workload.  Returns (net, opt, cells, dt).
+
+    Each cell starts from an equilibrium state (free ions drawn log-uniform in
+    [1e-7, 1e-3] mol/kg) and receives the totals of a perturbed state, free
+    ions scaled by exp(sigma * xi) with xi ~ N(0, 1) per species and sigma
+    log-uniform in `sigma_range`: the "transport update".  Both states must
+    have all totals in `tot_range`.  The previous-step guess is the
+    equilibrium state."""
     if net is None:
         net = synthetic_network()
     rng = np.random.default_rng(seed)
@@ -324,48 +357,43 @@ def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-3, 3.0), tot_range=(1e-
     sp = Speciator(net)
     N = net.N
     porosity, rho_s = 0.25, 2650.0
-    lnm = np.empty((0, N))
+    lo, hi = tot_range
+    keep_eq, keep_new, keep_sig = [], [], []
     have = 0
-    chunks = []
+    rounds = 0
     while have < n:
-        k = max(2 * (n - have), 1024)
-        cand = rng.uniform(np.log(1e-9), np.log(2e-3), (k, N))
-        I0 = np.full(k, 1e-2)
-        for _ in range(8):
-            lngp, lngc = sp.ln_gamma(I0)
-            Psi, Cc = sp.aqueous(cand, sp.logK, lngp, lngc)
-            I0 = sp.ionic_strength(cand, Cc)
-        tot = Psi * DEN_KG_25C * 1e-3
-        ok = np.all((tot >= tot_range[0]) & (tot <= tot_range[1]), axis=1) & (I0 < 1.0)
-        chunks.append(cand[ok])
+        rounds += 1
+        if rounds > 100:
+            raise RuntimeError("synthetic_cells: acceptance too low")
+        k = max(2 * (n - have), 4096)
+        lnm = rng.uniform(np.log(1e-7), np.log(3e-4), (k, N))
+        sig = 10.0 ** rng.uniform(np.log10(sigma_range[0]), np.log10(sigma_range[1]), k)
+        lnm2 = lnm + sig[:, None] * rng.standard_normal((k, N))
+        t1, _, I1, _ = _forward_state(sp, lnm, iters=6)
+        t2, _, I2, _ = _forward_state(sp, lnm2, iters=6)
+        with np.errstate(invalid="ignore"):
+            # |total| in range; only the H+-like species 0 may be negative
+            a1, a2 = np.abs(t1), np.abs(t2)
+            ok = (np.all((a1 >= lo) & (a1 <= hi), axis=1) & np.all((a2 >= lo) & (a2 <= hi), axis=1)
+                  & np.all(t1[:, 1:] > 0, axis=1) & np.all(t2[:, 1:] > 0, axis=1)
+                  & (I1 < 1.0) & (I2 < 1.0))
+        keep_eq.append(lnm[ok])
+        keep_new.append(lnm2[ok])
+        keep_sig.append(sig[ok])
         have += int(ok.sum())
-    lnm = np.concatenate(chunks)[:n]
+    lnm = np.concatenate(keep_eq)[:n]
+    lnm2 = np.concatenate(keep_new)[:n]
     b = CellBatch.allocate(net, n)
     _fill_common(b, n, porosity=porosity, rho_s=rho_s)
     b.temperature[:] = 25.0
-    den_L = b.den_kg * 1e-3
-    # self-consistent ionic strength of the equilibrium state
-    I = np.full(n, 1e-2)
-    for _ in range(60):
-        lngp, lngc = sp.ln_gamma(I)
-        Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
-        Inew = sp.ionic_strength(lnm, Cc)
-        if np.max(np.abs(Inew - I) / Inew) < 1e-15:
-            I = Inew
-            break
-        I = Inew
-    lngp, lngc = sp.ln_gamma(I)
-    Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
+    tot_eq, Cc, I, lngp = _forward_state(sp, lnm, iters=60)
+    tot_new, _, _, _ = _forward_state(sp, lnm2, iters=60)
     m = np.exp(lnm)
     vf = np.full((n, max(net.Nm, 1)), 1e-3)
     S, ref, free = sp.sorbed(m, np.exp(lngp), vf, porosity, rho_s)
-    # seeded log-normal transport update of the totals
-    sig = 10.0 ** rng.uniform(np.log10(sigma_range[0]), np.log10(sigma_range[1]), n)
-    xi = rng.standard_normal((n, N))
-    tot_eq = Psi * den_L[:, None]
-    b.view("total", N)[:] = (tot_eq * np.exp(sig[:, None] * xi)).T
+    b.view("total", N)[:] = tot_new.T
     b.view("pri_molal", N)[:] = m.T
-    b.ionic_strength[:] = sp.ionic_strength(lnm, Cc)
+    b.ionic_strength[:] = I
     b.mnrl_volfrac[:] = 1e-3
     b.mnrl_area[:] = 1.0
     if net.Nix + net.Nsr > 0:

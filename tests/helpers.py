@@ -1,0 +1,49 @@
+"""Shared helpers of the parity tests: workloads, scales and comparisons."""
+import numpy as np
+
+from pflotran_gb300 import abi
+from pflotran_gb300.workloads import Speciator
+
+
+def total_scale(net, cells):
+    """Per-component magnitude of the aqueous total: den_L*(m_j + sum_i |nu_ij| C_i)."""
+    sp = Speciator(net)
+    n = cells.ncells
+    m = cells.pri_molal.reshape(net.N, n)
+    if net.Nc:
+        C = cells.sec_molal.reshape(-1, n)[:net.Nc]
+        s = m + np.abs(sp.nu).T @ C
+    else:
+        s = m.copy()
+    return s * (cells.den_kg * 1e-3)[None, :]
+
+
+def rel_err(x, y, scale):
+    return np.abs(x - y) / np.maximum(np.abs(y), scale)
+
+
+def compare(net, gpu, ref, tol=1e-10, mask=None):
+    """Max scaled relative errors of the parity outputs (GPU vs oracle)."""
+    n = ref.ncells
+    if mask is None:
+        mask = np.ones(n, bool)
+    out = {}
+    out["pri_molal"] = rel_err(gpu.pri_molal.reshape(net.N, n), ref.pri_molal.reshape(net.N, n), 0.0)[:, mask].max()
+    sc = total_scale(net, ref)
+    out["total"] = rel_err(gpu.total_out.reshape(net.N, n), ref.total_out.reshape(net.N, n), sc)[:, mask].max()
+    if net.Nm:
+        k = np.array([mn.extra["k"] for mn in net.minerals])[:, None]
+        area = ref.mnrl_area.reshape(-1, n)[:net.Nm]
+        rs = k * area * 1e-12 + 1e-300  # scale: rate constant x area (x 1e-12 below which rates are noise)
+        rs = k * area
+        out["mnrl_rate"] = rel_err(gpu.mnrl_rate.reshape(-1, n)[:net.Nm], ref.mnrl_rate.reshape(-1, n)[:net.Nm],
+                                   rs)[:, mask].max()
+        out["mnrl_volfrac"] = rel_err(gpu.mnrl_volfrac.reshape(-1, n)[:net.Nm],
+                                      ref.mnrl_volfrac.reshape(-1, n)[:net.Nm], 1e-300)[:, mask].max()
+    if net.Nix + net.Nsr:
+        g = gpu.total_sorb_eq.reshape(net.N, n)
+        r = ref.total_sorb_eq.reshape(net.N, n)
+        s = np.maximum(np.abs(r).sum(0, keepdims=True) * 1e-6, 1e-300)
+        out["total_sorb_eq"] = rel_err(g, r, s)[:, mask].max()
+    out["ionic_strength"] = rel_err(gpu.ionic_strength, ref.ionic_strength, 0.0)[mask].max()
+    return out

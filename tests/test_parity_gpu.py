@@ -1,0 +1,203 @@
+"""GPU parity: the CUDA library against the oracle on identical seeded inputs.
+
+Tolerance: 1e-10 scaled relative error (|x - y| / max(|y|, s), with s the
+magnitude of the terms that make up the quantity) on free-ion molalities,
+aqueous totals, mineral rates and volume fractions, sorbed totals and ionic
+strength, at the headline convergence test (relative residual < 1e-12).
+"""
+import numpy as np
+import pytest
+
+from pflotran_gb300 import abi, workloads
+from pflotran_gb300.lib import PfchemError, ReactionStep
+from pflotran_gb300.network import default_options
+
+from helpers import compare
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-10
+
+
+def run_both(oracle, net, opt, cells, dt, device=True, nthreads=8):
+    ref = cells.copy()
+    if ref.sec_molal is None:
+        ref.sec_molal = np.zeros(max(net.Nc, 1) * cells.ncells)
+    gpu = ref.copy()
+    oracle.react(net.as_struct(), opt, dt, ref, 0, nthreads)
+    step = ReactionStep(net, opt)
+    if device:
+        d = gpu.to_device()
+        step.react(d, dt)
+        gpu = d.to_host()
+    else:
+        step.react(gpu, dt)
+    return ref, gpu, step
+
+
+def assert_parity(net, gpu, ref, tol=TOL, mask=None):
+    errs = compare(net, gpu, ref, mask=mask)
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, errs
+    return errs
+
+
+def test_calcite_column(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(100, seed=0)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    assert (ref.status == 0).all() and (gpu.status == 0).all()
+    assert_parity(net, gpu, ref)
+    assert np.mean(gpu.iterations == ref.iterations) > 0.95
+
+
+def test_calcite_grid_temperature_dependent(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(4096, seed=1, temperature_dependent=True)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    assert (gpu.status == 0).all()
+    assert_parity(net, gpu, ref)
+
+
+def test_synthetic_network(oracle):
+    net, opt, cells, dt = workloads.synthetic_cells(4096, seed=11)
+    ref, gpu, step = run_both(oracle, net, opt, cells, dt)
+    ok = (ref.status == 0) & (gpu.status == 0)
+    assert ok.mean() > 0.99, (np.bincount(ref.status), np.bincount(gpu.status))
+    assert_parity(net, gpu, ref, mask=ok)
+    st = step.stats()
+    assert st.ncells == 4096 and st.max_iterations == gpu.iterations.max()
+    assert st.sum_iterations == gpu.iterations.sum()
+
+
+def test_host_pointer_path(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(300, seed=2)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt, device=False)
+    assert_parity(net, gpu, ref)
+
+
+def test_interleaved_tran_xx_adapter(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(257, seed=3)
+    ref = cells.copy()
+    ref.sec_molal = np.zeros(net.Nc * cells.ncells)
+    oracle.react(net.as_struct(), opt, dt, ref, 0, 4)
+    ncomp = net.N + 2  # RTReact's tran_xx may carry immobile dofs after the aqueous ones
+    tran = np.zeros((cells.ncells, ncomp))
+    tran[:, :net.N] = cells.total.reshape(net.N, -1).T
+    tran[:, net.N:] = 7.0
+    gpu = cells.copy()
+    gpu.total = None
+    step = ReactionStep(net, opt)
+    d = gpu.to_device()
+    import torch
+    t = torch.from_numpy(tran.ravel().copy()).cuda()
+    step.react_interleaved(t, ncomp, d, dt)
+    out = t.cpu().numpy().reshape(cells.ncells, ncomp)
+    g = d.to_host()
+    assert np.allclose(out[:, :net.N].T.ravel(), g.pri_molal, rtol=0, atol=0)
+    assert (out[:, net.N:] == 7.0).all()
+    ref.total = cells.total
+    g.total = cells.total
+    assert_parity(net, g, ref)
+
+
+def test_reference_convergence_tests_literal_mode(oracle):
+    """RReact's own tests: absolute 1e-12 mol/s residual and 1e-6 relative
+    change, literal accumulation.  Cells whose iteration counts agree match."""
+    net, opt, cells, dt = workloads.calcite_cells(512, seed=4)
+    opt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                          accum_mode=abi.ACCUM_LITERAL, max_relative_change_tolerance=1e-6)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    same = gpu.iterations == ref.iterations
+    assert same.mean() > 0.98
+    assert_parity(net, gpu, ref, mask=same)
+
+
+def test_linear_formulation(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(256, seed=5)
+    opt.use_log_formulation = 0
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    ok = (ref.status == 0) & (gpu.status == 0)
+    assert ok.mean() > 0.98
+    assert_parity(net, gpu, ref, mask=ok)
+
+
+def test_newton_iteration_activity_update(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(256, seed=6)
+    opt.act_coef_update_frequency = abi.ACT_COEF_FREQUENCY_NEWTON_ITER
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    assert_parity(net, gpu, ref)
+
+
+def test_inactive_cells_are_skipped(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(200, seed=7)
+    cells.active = (np.arange(200) % 3 != 0).astype(np.int32)
+    before = cells.pri_molal.copy()
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    act = cells.active > 0
+    assert (gpu.status[~act] == abi.CELL_INACTIVE).all()
+    assert np.array_equal(gpu.pri_molal.reshape(3, -1)[:, ~act], before.reshape(3, -1)[:, ~act])
+    assert_parity(net, gpu, ref, mask=act)
+
+
+def test_alternative_guess_and_fallback(oracle):
+    net, opt, cells, dt = workloads.synthetic_cells(2048, seed=8)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    ok = (ref.status == 0)
+    # a perfect alternative guess is taken and converges at the first residual
+    c2 = cells.copy()
+    c2.alt_guess = ref.pri_molal.copy()
+    step = ReactionStep(net, opt)
+    d = c2.to_device()
+    step.react(d, dt)
+    g2 = d.to_host()
+    assert step.stats().alt_guess_used >= int(0.99 * ok.sum())
+    assert (g2.iterations[ok] <= 2).mean() > 0.99
+    assert_parity(net, g2, ref, mask=ok & (g2.status == 0))
+    # a bad alternative guess is rejected and the plain path's answer results
+    c3 = cells.copy()
+    c3.alt_guess = cells.pri_molal * 1e3
+    d = c3.to_device()
+    step.react(d, dt)
+    g3 = d.to_host()
+    assert step.stats().alt_guess_used < 0.05 * cells.ncells
+    assert_parity(net, g3, ref, mask=ok & (g3.status == 0))
+
+
+def test_update_kinetic_state_entry_point(oracle):
+    net, opt, cells, dt = workloads.calcite_cells(128, seed=9)
+    opt.update_kinetic_state = 0
+    ref, gpu, step = run_both(oracle, net, opt, cells, dt)
+    before = gpu.mnrl_volfrac.copy()
+    d = gpu.to_device()
+    step.update_kinetic_state(d, dt)
+    g = d.to_host()
+    exp = np.maximum(before + g.mnrl_rate * net.minerals[0].extra["Vm"] * dt, 0.0)
+    assert np.allclose(g.mnrl_volfrac, exp, rtol=1e-14, atol=0)
+
+
+def test_rejects_unsupported_networks():
+    from pflotran_gb300.network import ReactionNetwork
+    net = ReactionNetwork([(f"P{i}", 1.0, 4.0) for i in range(17)])
+    net.build()
+    with pytest.raises(PfchemError, match="naqcomp"):
+        ReactionStep(net, default_options())
+    net = workloads.calcite_network()
+    net.minerals[0].extra["pref"] = [dict(rate=1e-9, species=[("H+", 1.0, 0.0, 1.0)])]
+    net.build()
+    with pytest.raises(PfchemError, match="prefactors"):
+        ReactionStep(net, default_options())
+
+
+def test_calcite_grid_full_size_sampled(oracle):
+    """100^3 cells on the GPU; a seeded sample of 4000 cells re-solved by the oracle."""
+    net, opt, cells, dt = workloads.calcite_cells(1_000_000, seed=10, temperature_dependent=True)
+    step = ReactionStep(net, opt)
+    d = cells.to_device()
+    d.sec_molal = None
+    import torch
+    d.sec_molal = torch.zeros(net.Nc * cells.ncells, dtype=torch.float64, device="cuda")
+    assert step.react(d, dt) == 0
+    g = d.to_host()
+    idx = np.sort(np.random.default_rng(0).choice(cells.ncells, 4000, replace=False))
+    sub = cells.subset(idx, net)
+    sub.sec_molal = np.zeros(net.Nc * len(idx))
+    oracle.react(net.as_struct(), opt, dt, sub, 0, 8)
+    assert_parity(net, g.subset(idx, net), sub)
