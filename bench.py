@@ -106,10 +106,10 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_workload(ncells):
+def make_workload(ncells, device="cpu"):
     from pflotran_gb300 import workloads
     net = workloads.synthetic_network()
-    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024, net=net)
+    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024, net=net, device=device)
     return net, opt, cells, dt
 
 
@@ -128,11 +128,19 @@ def cpu_baseline(net, opt, cells, dt, sample):
                       f"{threads} std::threads"}, sub
 
 
+def _cuda():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
 def run_reference(args):
     rank, world, _ = rank_env()
     if rank != 0:
         return
-    net, opt, cells, dt = make_workload(args.ncells)
+    net, opt, cells, dt = make_workload(args.ncells, device="cuda" if _cuda() else "cpu")
     from oracle import oracle
     threads = os.cpu_count() or 1
     n = min(args.cpu_sample, cells.ncells)
@@ -175,7 +183,7 @@ def main():
     from pflotran_gb300.cells import CellBatch
     from pflotran_gb300.lib import ReactionStep
 
-    net, opt, host, dt = make_workload(args.ncells)
+    net, opt, host, dt = make_workload(args.ncells, device=f"cuda:{local}")
     n = host.ncells
     step = ReactionStep(net, opt, device=local)
     pristine = host.to_device()

@@ -144,131 +144,143 @@ def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rh
 
 
 # ---------------------------------------------------------------------------
-# host-side forward speciation (input generation)
+# forward speciation for input generation (torch, float64, CPU or CUDA)
 
 class Speciator:
-    """Vectorised RTotal / RTotalSorb at given free-ion molalities."""
+    """Vectorised RTotal / RTotalSorb at given free-ion molalities, used to
+    build consistent cell states.  Works on torch float64 tensors on any
+    device (a CUDA device generates millions of cells in seconds)."""
 
-    def __init__(self, net: ReactionNetwork):
+    def __init__(self, net: ReactionNetwork, device="cpu"):
+        import torch
+        self.torch = torch
+        self.dev = torch.device(device)
         self.net = net
         t = net._tables if net._tables is not None else net.build()
         self.t = t
         N, Nc = net.N, net.Nc
-        self.nu = np.zeros((Nc, N))
+        nu = np.zeros((Nc, N))
         ld = t["eqcplx_ld"]
         ids = t["eqcplxspecid"].reshape(-1, ld + 1)
         st = t["eqcplxstoich"].reshape(-1, ld)
         for i in range(Nc):
             for k in range(ids[i, 0]):
-                self.nu[i, ids[i, k + 1] - 1] = st[i, k]
-        self.h2o = t["eqcplxh2ostoich"][:Nc]
-        self.Zp, self.Zc = t["primary_spec_Z"], t["eqcplx_Z"][:Nc]
-        self.ap, self.ac = t["primary_spec_a0"], t["eqcplx_a0"][:Nc]
-        self.coef = t["eqcplx_logKcoef"].reshape(-1, 5)[:Nc]
-        self.logK = t["eqcplx_logK"][:Nc]
+                nu[i, ids[i, k + 1] - 1] = st[i, k]
+        self.nu_np = nu
+        T = lambda a: torch.as_tensor(np.asarray(a, dtype=np.float64), device=self.dev)
+        self.nu = T(nu)
+        self.Zp, self.Zc = T(t["primary_spec_Z"]), T(t["eqcplx_Z"][:Nc])
+        self.ap, self.ac = T(t["primary_spec_a0"]), T(t["eqcplx_a0"][:Nc])
+        self.coef = T(t["eqcplx_logKcoef"].reshape(-1, 5)[:Nc])
+        self.logK = T(t["eqcplx_logK"][:Nc])
+        self.T = T
 
-    def logK_at(self, T, isothermal):
+    def logK_at(self, temp, isothermal):
         if isothermal:
-            return np.broadcast_to(self.logK, (len(T), len(self.logK)))
-        tk = (T + 273.15)[:, None]
+            return self.logK.expand(len(temp), -1)
+        tk = (temp + 273.15)[:, None]
         c = self.coef
-        return c[:, 0] * np.log(tk) + c[:, 1] + c[:, 2] * tk + c[:, 3] / tk + c[:, 4] / (tk * tk)
+        return c[:, 0] * self.torch.log(tk) + c[:, 1] + c[:, 2] * tk + c[:, 3] / tk + c[:, 4] / (tk * tk)
 
     def ln_gamma(self, I):
         """LAG activity coefficients (reaction.F90:3992-4051) as ln gamma."""
+        torch = self.torch
         A, B, Bd = self.net.debye
-        s = np.sqrt(I)[:, None]
+        s = torch.sqrt(I)[:, None]
         lp = (-self.Zp ** 2 * s * A / (1.0 + self.ap * B * s) + Bd * I[:, None]) * LOG_TO_LN
         lc = (-self.Zc ** 2 * s * A / (1.0 + self.ac * B * s) + Bd * I[:, None]) * LOG_TO_LN
-        lp = np.where(np.abs(self.Zp) > 1e-10, lp, 0.0)
-        lc = np.where(np.abs(self.Zc) > 1e-10, lc, 0.0)
+        lp = torch.where(self.Zp.abs() > 1e-10, lp, torch.zeros_like(lp))
+        lc = torch.where(self.Zc.abs() > 1e-10, lc, torch.zeros_like(lc))
         return lp, lc
 
     def aqueous(self, lnm, logK, lngp, lngc):
         """molal totals Psi (n,N), complexes C (n,Nc)."""
         ln_act = lnm + lngp
         lnQK = -logK * LOG_TO_LN + ln_act @ self.nu.T
-        Cc = np.exp(lnQK - lngc)
-        Psi = np.exp(lnm) + Cc @ self.nu
+        Cc = self.torch.exp(lnQK - lngc)
+        Psi = self.torch.exp(lnm) + Cc @ self.nu
         return Psi, Cc
 
     def ionic_strength(self, lnm, Cc):
-        return 0.5 * (np.exp(lnm) @ (self.Zp ** 2) + Cc @ (self.Zc ** 2))
+        return 0.5 * (self.torch.exp(lnm) @ (self.Zp ** 2) + Cc @ (self.Zc ** 2))
 
-    def sorbed(self, m, gp, mnrl_volfrac, porosity, rho_s, ref_sorbed0=1e-9, free_site0=1e-9, logKsc=None):
+    def sorbed(self, m, gp, mnrl_volfrac, porosity, rho_s, ref_sorbed0=1e-9):
         """Equilibrium sorbed totals (mol/m^3 bulk) and the sorption warm
         starts, following RTotalSorbEqIonx (reaction.F90:4305-4535) and
-        RTotalSorbEqSurfCplx1 (reaction_surf_complex.F90:658-934)."""
+        RTotalSorbEqSurfCplx1 (reaction_surf_complex.F90:658-934) for unit
+        free-site stoichiometry."""
+        torch = self.torch
         net, t = self.net, self.t
         n, N = m.shape
-        S = np.zeros((n, N))
-        ref_out = np.zeros((n, net.Nix))
+        S = torch.zeros((n, N), dtype=torch.float64, device=self.dev)
+        ref_out = torch.zeros((n, max(net.Nix, 1)), dtype=torch.float64, device=self.dev)
         a = m * gp
         ldx = t["eqionx_ld"]
         xid = t["eqionx_rxn_cationid"].reshape(-1, ldx + 1)
         xk = t["eqionx_rxn_k"].reshape(-1, ldx)
+        Zp = t["primary_spec_Z"]
         for r in range(net.Nix):
-            nc = xid[r, 0]
-            ids = xid[r, 1:nc + 1] - 1
-            ks = xk[r, :nc]
-            Zs = self.Zp[ids]
-            to = t["eqionx_rxn_to_surf"][r]
-            omega = t["eqionx_rxn_CEC"][r] * (np.maximum(mnrl_volfrac[:, to - 1], 1e-40) if to > 0 else 1.0)
-            omega = np.broadcast_to(omega, (n,))
+            nc = int(xid[r, 0])
+            ids = [int(x) - 1 for x in xid[r, 1:nc + 1]]
+            ks = [float(x) for x in xk[r, :nc]]
+            Zs = [float(Zp[i]) for i in ids]
+            to = int(t["eqionx_rxn_to_surf"][r])
+            omega = float(t["eqionx_rxn_CEC"][r])
+            omega = omega * torch.clamp(mnrl_volfrac[:, to - 1], min=1e-40) if to > 0 else \
+                torch.full((n,), omega, dtype=torch.float64, device=self.dev)
             if t["eqionx_rxn_Z_flag"][r]:
                 ref = ks[0] * a[:, ids[0]]
                 KD = (Zs[0] * ref_sorbed0 / omega) / ref
                 for _ in range(200):
                     tot = KD * ref
-                    d = ref.copy()
+                    d = ref.clone()
                     for j in range(1, nc):
                         x = ks[j] * a[:, ids[j]] * KD ** (Zs[j] / Zs[0])
                         tot = tot + x
                         d = d + x / KD * Zs[j] / Zs[0]
                     step = (1.0 - tot) / d
-                    KD = np.maximum(KD + step, 1e-40)
-                    if np.all(np.abs(step / KD) < 1e-13):
+                    KD = torch.clamp(KD + step, min=1e-40)
+                    if bool(torch.all((step / KD).abs() < 1e-13)):
                         break
                 X = [KD * ref] + [ks[j] * a[:, ids[j]] * KD ** (Zs[j] / Zs[0]) for j in range(1, nc)]
                 ref_out[:, r] = X[0] * omega / Zs[0]
             else:
                 X = [ks[j] * a[:, ids[j]] for j in range(nc)]
-                s = sum(X)
-                X = [x / s for x in X]
+                ssum = sum(X)
+                X = [x / ssum for x in X]
                 ref_out[:, r] = ref_sorbed0
             for j in range(nc):
                 S[:, ids[j]] += X[j] * omega / Zs[j]
-        free_out = np.zeros((n, net.Nsr))
+        free_out = torch.zeros((n, max(net.Nsr, 1)), dtype=torch.float64, device=self.dev)
         ldr, lds = t["srfcplxrxn_ld"], t["srfcplx_ld"]
         r2c = t["srfcplxrxn_to_complex"].reshape(-1, ldr + 1)
         sid = t["srfcplxspecid"].reshape(-1, lds + 1)
         sst = t["srfcplxstoich"].reshape(-1, lds)
-        lnact = np.log(a)
+        lnact = torch.log(a)
         for r in range(net.Nsr):
-            stype = t["srfcplxrxn_surf_type"][r]
-            dens = t["srfcplxrxn_site_density"][r]
+            stype = int(t["srfcplxrxn_surf_type"][r])
+            dens = float(t["srfcplxrxn_site_density"][r])
             if stype == abi.ROCK_SURFACE:
                 site = dens * rho_s * (1.0 - porosity)
             elif stype == abi.MINERAL_SURFACE:
-                site = dens * mnrl_volfrac[:, t["srfcplxrxn_to_surf"][r] - 1]
+                site = dens * mnrl_volfrac[:, int(t["srfcplxrxn_to_surf"][r]) - 1]
             else:
-                site = np.full(n, dens)
-            site = np.broadcast_to(site, (n,))
+                site = dens
             terms = []
-            for j in range(r2c[r, 0]):
-                ic = r2c[r, j + 1] - 1
-                lq = -t["srfcplx_logK"][ic] * LOG_TO_LN
-                lq = lq + sum(sst[ic, k] * lnact[:, sid[ic, k + 1] - 1] for k in range(sid[ic, 0]))
+            for j in range(int(r2c[r, 0])):
+                ic = int(r2c[r, j + 1]) - 1
+                lq = -float(t["srfcplx_logK"][ic]) * LOG_TO_LN
+                for k in range(int(sid[ic, 0])):
+                    lq = lq + float(sst[ic, k]) * lnact[:, int(sid[ic, k + 1]) - 1]
                 terms.append((ic, lq))
-            # free-site stoichiometry 1: closed form Sx = site / (1 + sum K_i a^nu)
-            ratio = sum(np.exp(lq) for _, lq in terms)
+            ratio = sum(torch.exp(lq) for _, lq in terms)
             free = site / (1.0 + ratio)
             free_out[:, r] = free
             for ic, lq in terms:
-                Sc = np.exp(lq) * free
-                for k in range(sid[ic, 0]):
-                    S[:, sid[ic, k + 1] - 1] += sst[ic, k] * Sc
-        return S, ref_out, free_out
+                Sc = torch.exp(lq) * free
+                for k in range(int(sid[ic, 0])):
+                    S[:, int(sid[ic, k + 1]) - 1] += float(sst[ic, k]) * Sc
+        return S, ref_out[:, :net.Nix], free_out[:, :net.Nsr]
 
 
 def _fill_common(b, n, porosity=0.25, sat=1.0, volume=1.0, den=DEN_KG_25C, rho_s=2650.0):
@@ -279,127 +291,141 @@ def _fill_common(b, n, porosity=0.25, sat=1.0, volume=1.0, den=DEN_KG_25C, rho_s
     b.soil_particle_density[:] = rho_s
 
 
-def calcite_cells(n=100, seed=0, temperature_dependent=False, net=None):
+def _np(x):
+    return x.detach().cpu().numpy()
+
+
+def calcite_cells(n=100, seed=0, temperature_dependent=False, net=None, device="cpu"):
     """Calcite column (25 C) or, with temperature_dependent, the calcite grid
     workload with T ~ U[10, 60] C.  Returns (net, opt, cells, dt)."""
+    import torch
     rng = np.random.default_rng(seed)
     if net is None:
         net = calcite_network(temperature_dependent=temperature_dependent, seed=seed)
     opt = default_options(use_isothermal=0 if temperature_dependent else 1)
-    sp = Speciator(net)
+    sp = Speciator(net, device)
     b = CellBatch.allocate(net, n)
     _fill_common(b, n)
     T = rng.uniform(10.0, 60.0, n) if temperature_dependent else np.full(n, 25.0)
     b.temperature[:] = T
-    tCa = 10.0 ** rng.uniform(-5.0, -2.0, n)
-    tC = 10.0 ** rng.uniform(-5.0, -2.0, n)
-    pH = rng.uniform(5.0, 9.0, n)
-    den_L = b.den_kg * 1e-3
-    logK = sp.logK_at(T, opt.use_isothermal)
+    tCa = sp.T(10.0 ** rng.uniform(-5.0, -2.0, n))
+    tC = sp.T(10.0 ** rng.uniform(-5.0, -2.0, n))
+    pH = sp.T(rng.uniform(5.0, 9.0, n))
+    den_L = sp.T(b.den_kg * 1e-3)
+    logK = sp.logK_at(sp.T(T), opt.use_isothermal)
     # constraint speciation: pH row for H+, TOTAL rows for HCO3- and Ca++
-    lnm = np.stack([-pH * LOG_TO_LN, np.log(tC / den_L), np.log(tCa / den_L)], axis=1)
-    I = np.full(n, 1e-3)
+    lnm = torch.stack([-pH * LOG_TO_LN, torch.log(tC / den_L), torch.log(tCa / den_L)], dim=1)
+    I = torch.full((n,), 1e-3, dtype=torch.float64, device=sp.dev)
+    eye = torch.eye(3, dtype=torch.float64, device=sp.dev)
     for outer in range(30):
         lngp, lngc = sp.ln_gamma(I)
         lnm[:, 0] = -pH * LOG_TO_LN - lngp[:, 0]
         for it in range(60):
             Psi, Cc = sp.aqueous(lnm, logK, lngp, lngc)
-            F = Psi[:, 1:] * den_L[:, None] - np.stack([tC, tCa], 1)
+            F = Psi[:, 1:] * den_L[:, None] - torch.stack([tC, tCa], 1)
             # d Psi_j / d ln m_k = m_j delta_jk + sum_i nu_ij nu_ik C_i
-            Jf = np.einsum("ij,ik,ni->njk", sp.nu, sp.nu, Cc) + np.einsum("jk,nj->njk", np.eye(3), np.exp(lnm))
+            Jf = torch.einsum("ij,ik,ni->njk", sp.nu, sp.nu, Cc) + torch.einsum("jk,nj->njk", eye, torch.exp(lnm))
             J = Jf[:, 1:, 1:] * den_L[:, None, None]
-            d = np.linalg.solve(J, F[..., None])[..., 0]
-            d = np.clip(d, -2.0, 2.0)
+            d = torch.linalg.solve(J, F[..., None])[..., 0]
+            d = torch.clamp(d, -2.0, 2.0)
             lnm[:, 1:] -= d
-            if np.max(np.abs(d)) < 1e-14:
+            if float(d.abs().max()) < 1e-14:
                 break
         Inew = sp.ionic_strength(lnm, Cc)
-        if np.max(np.abs(Inew - I) / Inew) < 1e-15:
+        if float(((Inew - I).abs() / Inew).max()) < 1e-15:
             I = Inew
             break
         I = Inew
     lngp, lngc = sp.ln_gamma(I)
     Psi, Cc = sp.aqueous(lnm, logK, lngp, lngc)
-    b.view("total", net.N)[:] = (Psi * den_L[:, None]).T
-    b.view("pri_molal", net.N)[:] = np.exp(lnm).T
-    b.ionic_strength[:] = sp.ionic_strength(lnm, Cc)
+    b.view("total", net.N)[:] = _np((Psi * den_L[:, None]).T)
+    b.view("pri_molal", net.N)[:] = _np(torch.exp(lnm).T)
+    b.ionic_strength[:] = _np(sp.ionic_strength(lnm, Cc))
     b.mnrl_volfrac[:] = 1e-5
     b.mnrl_area[:] = 1.0
     dt = 86400.0 if temperature_dependent else 3600.0
     return net, opt, b, dt
 
 
-def _forward_state(sp, lnm, iters=12):
-    """Totals (mol/L), complexes and the self-consistent ionic strength at free ions exp(lnm)."""
+def _forward_state(sp, lnm, iters=12, tol=None):
+    """Totals (mol/L), complexes and the self-consistent ionic strength at
+    free ions exp(lnm)."""
+    torch = sp.torch
     n = lnm.shape[0]
-    I = np.full(n, 1e-3)
-    with np.errstate(all="ignore"):
-        for _ in range(iters):
-            lngp, lngc = sp.ln_gamma(np.clip(I, 0.0, 10.0))
-            Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
-            I = sp.ionic_strength(lnm, Cc)
+    I = torch.full((n,), 1e-3, dtype=torch.float64, device=sp.dev)
+    for _ in range(iters):
+        lngp, lngc = sp.ln_gamma(torch.clamp(I, 0.0, 10.0))
+        Psi, Cc = sp.aqueous(lnm, sp.logK, lngp, lngc)
+        Inew = sp.ionic_strength(lnm, Cc)
+        done = tol is not None and bool(torch.all(((Inew - I).abs() <= tol * Inew) | ~torch.isfinite(Inew)))
+        I = Inew
+        if done:
+            break
     return Psi * DEN_KG_25C * 1e-3, Cc, I, lngp
 
 
-def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-2, 2.0), tot_range=(1e-10, 1e-1)):
+def synthetic_cells(n, seed=5, net=None, sigma_range=(1e-2, 2.0), tot_range=(1e-10, 1e-1), device="cpu"):
     """Cells of the synthetic 12-species workload.  Returns (net, opt, cells, dt).
 
     Each cell starts from an equilibrium state (free ions drawn log-uniform in
-    [1e-7, 1e-3] mol/kg) and receives the totals of a perturbed state, free
+    [1e-7, 3e-4] mol/kg) and receives the totals of a perturbed state, free
     ions scaled by exp(sigma * xi) with xi ~ N(0, 1) per species and sigma
     log-uniform in `sigma_range`: the "transport update".  Both states must
-    have all totals in `tot_range`.  The previous-step guess is the
-    equilibrium state."""
+    have all |totals| in `tot_range` (only the H+-like species 0 may have a
+    negative total).  The previous-step guess is the equilibrium state.
+    Random numbers come from a torch.Generator seeded with `seed` on `device`."""
+    import torch
     if net is None:
         net = synthetic_network()
-    rng = np.random.default_rng(seed)
     opt = default_options(use_isothermal=1)
-    sp = Speciator(net)
+    sp = Speciator(net, device)
+    g = torch.Generator(device=sp.dev)
+    g.manual_seed(seed)
     N = net.N
     porosity, rho_s = 0.25, 2650.0
     lo, hi = tot_range
-    keep_eq, keep_new, keep_sig = [], [], []
+    keep_eq, keep_new = [], []
     have = 0
     rounds = 0
+    l1, l2 = float(np.log(1e-7)), float(np.log(3e-4))
+    s1, s2 = float(np.log10(sigma_range[0])), float(np.log10(sigma_range[1]))
     while have < n:
         rounds += 1
         if rounds > 100:
             raise RuntimeError("synthetic_cells: acceptance too low")
         k = max(2 * (n - have), 4096)
-        lnm = rng.uniform(np.log(1e-7), np.log(3e-4), (k, N))
-        sig = 10.0 ** rng.uniform(np.log10(sigma_range[0]), np.log10(sigma_range[1]), k)
-        lnm2 = lnm + sig[:, None] * rng.standard_normal((k, N))
+        u = torch.rand((k, N), generator=g, dtype=torch.float64, device=sp.dev)
+        lnm = l1 + (l2 - l1) * u
+        sig = 10.0 ** (s1 + (s2 - s1) * torch.rand((k,), generator=g, dtype=torch.float64, device=sp.dev))
+        xi = torch.randn((k, N), generator=g, dtype=torch.float64, device=sp.dev)
+        lnm2 = lnm + sig[:, None] * xi
         t1, _, I1, _ = _forward_state(sp, lnm, iters=6)
         t2, _, I2, _ = _forward_state(sp, lnm2, iters=6)
-        with np.errstate(invalid="ignore"):
-            # |total| in range; only the H+-like species 0 may be negative
-            a1, a2 = np.abs(t1), np.abs(t2)
-            ok = (np.all((a1 >= lo) & (a1 <= hi), axis=1) & np.all((a2 >= lo) & (a2 <= hi), axis=1)
-                  & np.all(t1[:, 1:] > 0, axis=1) & np.all(t2[:, 1:] > 0, axis=1)
-                  & (I1 < 1.0) & (I2 < 1.0))
+        a1, a2 = t1.abs(), t2.abs()
+        ok = (torch.all((a1 >= lo) & (a1 <= hi), dim=1) & torch.all((a2 >= lo) & (a2 <= hi), dim=1)
+              & torch.all(t1[:, 1:] > 0, dim=1) & torch.all(t2[:, 1:] > 0, dim=1) & (I1 < 1.0) & (I2 < 1.0))
         keep_eq.append(lnm[ok])
         keep_new.append(lnm2[ok])
-        keep_sig.append(sig[ok])
         have += int(ok.sum())
-    lnm = np.concatenate(keep_eq)[:n]
-    lnm2 = np.concatenate(keep_new)[:n]
+    lnm = torch.cat(keep_eq)[:n]
+    lnm2 = torch.cat(keep_new)[:n]
     b = CellBatch.allocate(net, n)
     _fill_common(b, n, porosity=porosity, rho_s=rho_s)
     b.temperature[:] = 25.0
-    tot_eq, Cc, I, lngp = _forward_state(sp, lnm, iters=60)
-    tot_new, _, _, _ = _forward_state(sp, lnm2, iters=60)
-    m = np.exp(lnm)
-    vf = np.full((n, max(net.Nm, 1)), 1e-3)
-    S, ref, free = sp.sorbed(m, np.exp(lngp), vf, porosity, rho_s)
-    b.view("total", N)[:] = tot_new.T
-    b.view("pri_molal", N)[:] = m.T
-    b.ionic_strength[:] = I
+    tot_eq, Cc, I, lngp = _forward_state(sp, lnm, iters=100, tol=1e-15)
+    tot_new, _, _, _ = _forward_state(sp, lnm2, iters=100, tol=1e-15)
+    m = torch.exp(lnm)
+    vf = torch.full((n, max(net.Nm, 1)), 1e-3, dtype=torch.float64, device=sp.dev)
+    S, ref, free = sp.sorbed(m, torch.exp(lngp), vf, porosity, rho_s)
+    b.view("total", N)[:] = _np(tot_new.T)
+    b.view("pri_molal", N)[:] = _np(m.T)
+    b.ionic_strength[:] = _np(I)
     b.mnrl_volfrac[:] = 1e-3
     b.mnrl_area[:] = 1.0
     if net.Nix + net.Nsr > 0:
-        b.view("total_sorb_eq", N)[:] = S.T
+        b.view("total_sorb_eq", N)[:] = _np(S.T)
     if net.Nix > 0:
-        b.view("eqionx_ref_cation_sorbed_conc", net.Nix)[:] = ref.T
+        b.view("eqionx_ref_cation_sorbed_conc", net.Nix)[:] = _np(ref.T)
     if net.Nsr > 0:
-        b.view("srfcplxrxn_free_site_conc", net.Nsr)[:] = free.T
+        b.view("srfcplxrxn_free_site_conc", net.Nsr)[:] = _np(free.T)
     return net, opt, b, 86400.0

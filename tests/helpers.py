@@ -7,12 +7,12 @@ from pflotran_gb300.workloads import Speciator
 
 def total_scale(net, cells):
     """Per-component magnitude of the aqueous total: den_L*(m_j + sum_i |nu_ij| C_i)."""
-    sp = Speciator(net)
+    nu = Speciator(net).nu_np
     n = cells.ncells
     m = cells.pri_molal.reshape(net.N, n)
     if net.Nc:
         C = cells.sec_molal.reshape(-1, n)[:net.Nc]
-        s = m + np.abs(sp.nu).T @ C
+        s = m + np.abs(nu).T @ C
     else:
         s = m.copy()
     return s * (cells.den_kg * 1e-3)[None, :]
