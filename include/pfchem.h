@@ -26,6 +26,7 @@
 #ifndef PFCHEM_H
 #define PFCHEM_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -266,6 +267,29 @@ int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
 /* Times candidate mappings on `cells` (device pointers; the state arrays are
  * restored after every trial) and keeps the fastest. */
 int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+/* Size of the library's static device scratch used by
+ * pfchem_react_batch_noalloc: a 256-byte work-queue head plus 32 bytes per
+ * thread block of the solve (at most 2040 blocks). */
+#define PFCHEM_NOALLOC_SCRATCH_BYTES 65536
+
+/* No counterpart in the reference.  The batched reaction step for callers
+ * that may not allocate device memory -- codes whose device memory all comes
+ * from their own pool (PETSc/Kokkos pools, a coupling framework's arena) or
+ * that cannot afford cudaMalloc's device synchronisation inside a time step.
+ * No context is needed: the call flattens `net`/`opt`, solves all cells of
+ * `cells` (device pointers only, on_device = 1) on `stream` (a cudaStream_t,
+ * NULL = default stream) and waits for it.  It calls no cudaMalloc/cudaFree;
+ * its only global scratch is a static device array of
+ * PFCHEM_NOALLOC_SCRATCH_BYTES bytes, held by every GPU that loads the
+ * library until exit, and launches needing more are rejected (-1, message in
+ * err).  The first call on a device looks up that array's address; make it
+ * before any stream capture.  All calls share the array: calls that overlap
+ * on the GPU race, so serialise them.  `stats` may be NULL (kernel_ms is not
+ * measured).  Returns as pfchem_react_batch; error text goes to err[errlen]. */
+int pfchem_react_batch_noalloc(const pfchem_network *net, const pfchem_options *opt, double dt,
+                               pfchem_cells *cells, void *stream, pfchem_stats *stats, char *err,
+                               size_t errlen);
 
 #ifdef __cplusplus
 }

@@ -405,6 +405,17 @@ int react_host(pfchem_ctx *c, double dt, pfchem_cells *cl, double *tran_xx, int3
 
 }  // namespace
 
+namespace pfchem {
+// Flattens and validates a network (used by the allocation-free entry point).
+int flatten_network(const pfchem_network *w, const pfchem_options *o, DevNet &n, char *err, size_t errlen) {
+  pfchem_ctx tmp;
+  int r = build_devnet(&tmp, w, o, n);
+  if (r && err && errlen) snprintf(err, errlen, "%s", tmp.err);
+  return r;
+}
+CellArgs cell_args(const pfchem_cells *cl, double dt) { return device_args(cl, dt); }
+}  // namespace pfchem
+
 extern "C" {
 
 int pfchem_create(pfchem_ctx **out, int device) {

@@ -718,6 +718,98 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
   }
 }
 
+// Variant of react_kernel whose scratch is a caller-supplied block of global
+// memory: the work-queue head, then one statistics slot per block (the
+// blocks' warps add into their own slot, so the host needs no other buffer).
+struct BlockSlot {
+  unsigned long long sum_iter, alt_used;
+  unsigned int max_iter, nonconverged;
+  unsigned long long pad;
+};
+
+template <class S>
+__global__ void __launch_bounds__(256) react_kernel_slots(const __grid_constant__ DevNet n,
+                                                          const __grid_constant__ CellArgs a,
+                                                          unsigned long long *queue_head, BlockSlot *slots,
+                                                          int refill_min_idle, double inv_dt) {
+  extern __shared__ double smem[];
+  double *J = smem + threadIdx.x;
+  const int js = blockDim.x;
+  const unsigned full = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  Lane<S> L;
+  int64_t cell = -1;
+  bool exhausted = false;
+  unsigned long long my_iters = 0, my_alt = 0;
+  unsigned my_max = 0, my_bad = 0;
+  for (;;) {
+    const bool want = (cell < 0) && !exhausted;
+    const unsigned want_mask = __ballot_sync(full, want);
+    const unsigned busy_mask = __ballot_sync(full, cell >= 0);
+    const int nwant = __popc(want_mask);
+    if (nwant > 0 && (nwant >= refill_min_idle || busy_mask == 0)) {
+      const int leader = __ffs(want_mask) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(queue_head, (unsigned long long)nwant);
+      base = __shfl_sync(full, base, leader);
+      if (want) {
+        const unsigned long long c = base + __popc(want_mask & ((1u << lane) - 1u));
+        if (c < (unsigned long long)a.ncells) {
+          cell = (int64_t)c;
+          if (a.active && a.active[cell] <= 0) {
+            if (a.status) a.status[cell] = PFCHEM_CELL_INACTIVE;
+            if (a.iters) a.iters[cell] = 0;
+            cell = -1;
+          } else {
+            setup(n, a, cell, L, inv_dt);
+            if (a.alt_guess) arm_alt_guess(n, a, cell, L);
+          }
+        } else {
+          exhausted = true;
+        }
+      }
+      continue;
+    }
+    if (busy_mask == 0) {
+      if (__all_sync(full, exhausted)) break;
+      continue;
+    }
+    if (cell >= 0) {
+      int st = newton_step(n, L, J, js);
+      if (st == -2) {
+        for (int j = 0; j < n.N; ++j) {
+          L.m[j] = a.pri_molal[j * a.ncells + cell];
+          L.lnm[j] = log(L.m[j]);
+        }
+        L.iter = 0;
+        for (int r = 0; r < n.Nix; ++r) L.ixref[r] = a.ixref[r * a.ncells + cell];
+        st = -1;
+      }
+      if (st >= 0) {
+        my_alt += L.alt_used ? 1 : 0;
+        finalize(n, a, cell, L, st);
+        my_iters += L.iter;
+        my_max = max(my_max, (unsigned)L.iter);
+        if (st != PFCHEM_CELL_CONVERGED) my_bad += 1;
+        cell = -1;
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    my_iters += __shfl_xor_sync(full, my_iters, o);
+    my_alt += __shfl_xor_sync(full, my_alt, o);
+    my_max = max(my_max, __shfl_xor_sync(full, my_max, o));
+    my_bad += __shfl_xor_sync(full, my_bad, o);
+  }
+  if (lane == 0) {
+    BlockSlot *sl = slots + blockIdx.x;
+    atomicAdd(&sl->sum_iter, my_iters);
+    atomicAdd(&sl->alt_used, my_alt);
+    atomicMax(&sl->max_iter, my_max);
+    atomicAdd(&sl->nonconverged, my_bad);
+  }
+}
+
 template <class S>
 __global__ void __launch_bounds__(256) kinetic_state_kernel(const __grid_constant__ DevNet n,
                                                             const __grid_constant__ CellArgs a) {
@@ -802,4 +894,64 @@ int max_active_blocks(const DevNet &n, int block) {
   }
 }
 
+
+template <class S>
+static int slots_blocks_per_sm_t(int block, size_t shm) {
+  int nb = 0;
+  if (cudaFuncSetAttribute(react_kernel_slots<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024) !=
+      cudaSuccess)
+    return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, react_kernel_slots<S>, block, shm) != cudaSuccess) return 0;
+  return nb;
+}
+
+// Resident blocks per SM of react_kernel_slots for `block` threads (0 if it
+// does not fit).  Sets the kernel's dynamic shared-memory limit.
+int slots_blocks_per_sm(const DevNet &n, int block) {
+  const size_t shm = (size_t)n.N * n.N * block * sizeof(double);
+  switch (size_class(n)) {
+    case 0: return slots_blocks_per_sm_t<SizesS>(block, shm);
+    case 1: return slots_blocks_per_sm_t<SizesM>(block, shm);
+    default: return slots_blocks_per_sm_t<SizesL>(block, shm);
+  }
+}
+
+size_t slots_scratch_bytes(int grid) { return 256 + (size_t)grid * sizeof(BlockSlot); }
+
+template <class S>
+static cudaError_t launch_slots_t(const DevNet &n, const CellArgs &a, void *scratch, int grid, int block,
+                                  int refill, cudaStream_t st) {
+  const size_t shm = (size_t)n.N * n.N * block * sizeof(double);
+  unsigned long long *head = (unsigned long long *)scratch;
+  BlockSlot *slots = (BlockSlot *)((char *)scratch + 256);
+  react_kernel_slots<S><<<grid, block, shm, st>>>(n, a, head, slots, refill, 1.0 / a.dt);
+  return cudaGetLastError();
+}
+
+// Launches react_kernel_slots with its queue head and statistics slots in
+// `scratch` (slots_scratch_bytes(grid) bytes, zeroed by the caller).
+cudaError_t launch_react_slots(const DevNet &n, const CellArgs &a, void *scratch, int grid, int block, int refill,
+                               cudaStream_t st) {
+  switch (size_class(n)) {
+    case 0: return launch_slots_t<SizesS>(n, a, scratch, grid, block, refill, st);
+    case 1: return launch_slots_t<SizesM>(n, a, scratch, grid, block, refill, st);
+    default: return launch_slots_t<SizesL>(n, a, scratch, grid, block, refill, st);
+  }
+}
+
+// Sums the per-block slots read back to the host.
+void sum_slots(const void *host_slots, int grid, unsigned long long *sum_iter, unsigned long long *alt,
+               unsigned *max_iter, unsigned *bad) {
+  const BlockSlot *sl = (const BlockSlot *)host_slots;
+  *sum_iter = 0;
+  *alt = 0;
+  *max_iter = 0;
+  *bad = 0;
+  for (int b = 0; b < grid; ++b) {
+    *sum_iter += sl[b].sum_iter;
+    *alt += sl[b].alt_used;
+    *max_iter = sl[b].max_iter > *max_iter ? sl[b].max_iter : *max_iter;
+    *bad += sl[b].nonconverged;
+  }
+}
 }  // namespace pfchem
