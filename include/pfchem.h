@@ -260,13 +260,23 @@ typedef struct pfchem_launch {
   int32_t block_threads;    /* threads per block                         */
   int32_t blocks_per_sm;    /* resident blocks per SM for the persistent grid */
   int32_t refill_min_idle;  /* lanes idle in a warp before they fetch new cells */
-  int32_t reserved3;
+  int32_t variant;          /* PFCHEM_KERNEL_* */
 } pfchem_launch;
+#define PFCHEM_KERNEL_SPECIALIZED 0 /* network-specialized kernel compiled at set_network (default) */
+#define PFCHEM_KERNEL_GENERIC 1     /* table-driven kernel compiled into the library */
 int pfchem_get_launch(const pfchem_ctx *ctx, pfchem_launch *launch);
 int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
 /* Times candidate mappings on `cells` (device pointers; the state arrays are
  * restored after every trial) and keeps the fastest. */
 int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+/* Generates and compiles (NVRTC, sm_103a) the network-specialized solve
+ * kernel for `net`/`opt` with `block_threads` threads per block, without
+ * loading it; needs no GPU.  Returns 0 or < 0 with the compiler log in
+ * log[loglen].  No counterpart in the reference: a build-time check of a
+ * network for the specialized path. */
+int pfchem_check_specialized(const pfchem_network *net, const pfchem_options *opt, int block_threads,
+                             char *log, size_t loglen);
 
 /* Size of the library's static device scratch used by
  * pfchem_react_batch_noalloc: a 256-byte work-queue head plus 32 bytes per

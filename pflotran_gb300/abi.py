@@ -38,6 +38,9 @@ CELL_NONFINITE = 3
 CELL_INNER_MAXITER = 4
 CELL_INACTIVE = 5
 
+KERNEL_SPECIALIZED = 0
+KERNEL_GENERIC = 1
+
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
 
@@ -112,7 +115,7 @@ class Stats(C.Structure):
 class Launch(C.Structure):
     _fields_ = [
         ("block_threads", C.c_int32), ("blocks_per_sm", C.c_int32),
-        ("refill_min_idle", C.c_int32), ("reserved3", C.c_int32),
+        ("refill_min_idle", C.c_int32), ("variant", C.c_int32),
     ]
 
 

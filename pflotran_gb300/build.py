@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpfchem.so")
 PROBE = os.path.join(OUT, "libpfchem_probe.so")
-SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu"]
+SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu", "pfchem_codegen.cu"]
 PROBE_SOURCES = ["fp64_peak.cu"]
 HEADERS = ["pfchem_device.cuh", os.path.join("..", "..", "include", "pfchem.h")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
@@ -26,6 +26,10 @@ def _nvcc():
         if c and (os.path.sep not in c or os.path.exists(c)):
             return c
     return "nvcc"
+
+
+def _cuda_home():
+    return os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 
 def _digest():
@@ -61,6 +65,9 @@ def build(force=False, verbose=False):
     for target, o in ((LIB, objs[:len(SOURCES)]), (PROBE, objs[len(SOURCES):])):
         tmp = target + ".tmp"
         cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + o
+        if target == LIB:
+            cmd += ["-L" + os.path.join(_cuda_home(), "lib64"),
+                    "-lnvrtc"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stderr}")

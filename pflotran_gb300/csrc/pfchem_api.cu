@@ -11,7 +11,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
+#include <nvrtc.h>
 
 #include "../../include/pfchem.h"
 #include "pfchem_device.cuh"
@@ -21,6 +23,12 @@ cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int g
                          cudaStream_t st);
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
+int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err);
+int gen_blocks_per_sm(void *fn, const DevNet &n, int block);
+size_t gen_shared_bytes(const DevNet &n, int block);
+std::string generate_source(const DevNet &n, int block);
+cudaError_t gen_launch(void *fn, const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
+                       cudaStream_t st);
 }  // namespace pfchem
 
 using namespace pfchem;
@@ -47,7 +55,9 @@ struct pfchem_ctx {
   cudaGraphExec_t graph = nullptr;
   CellArgs graph_args{};
   pfchem_launch graph_launch{};
-  char err[512] = {0};
+  void *gen_fn = nullptr;  // specialized kernel for gen_block threads per block
+  int gen_block = 0;
+  char err[2048] = {0};
 };
 
 namespace {
@@ -234,6 +244,37 @@ void default_launch(pfchem_ctx *c) {
   int nb = max_active_blocks(c->net, 64);
   c->launch.blocks_per_sm = std::max(1, nb);
   c->launch.refill_min_idle = 8;
+  c->launch.variant = PFCHEM_KERNEL_GENERIC;
+}
+
+// Compiles (or reuses) the network-specialized kernel for `block` threads per
+// block and returns its resident blocks per SM (0 on failure, message in err).
+int ensure_gen(pfchem_ctx *c, int block) {
+  if (c->gen_fn && c->gen_block == block) return gen_blocks_per_sm(c->gen_fn, c->net, block);
+  std::string e;
+  void *fn = nullptr;
+  if (gen_kernel(c->net, block, &fn, &e) != 0) {
+    fail(c, -2, "specialized kernel: %s", e.c_str());
+    return 0;
+  }
+  c->gen_fn = fn;
+  c->gen_block = block;
+  int nb = gen_blocks_per_sm(fn, c->net, block);
+  if (nb < 1) fail(c, -1, "specialized kernel with %d threads per block does not fit on an SM", block);
+  return nb;
+}
+
+// Specialized kernel, 32 threads per block, as many blocks per SM as fit,
+// refill when 8 lanes of a warp are idle.
+int default_specialized_launch(pfchem_ctx *c) {
+  const int block = 32;
+  int nb = ensure_gen(c, block);
+  if (nb < 1) return -2;
+  c->launch.block_threads = block;
+  c->launch.blocks_per_sm = nb;
+  c->launch.refill_min_idle = 8;
+  c->launch.variant = PFCHEM_KERNEL_SPECIALIZED;
+  return 0;
 }
 
 int check_cells(pfchem_ctx *c, const pfchem_cells *cl) {
@@ -307,7 +348,9 @@ int run_solve(pfchem_ctx *c, const CellArgs &a) {
     cudaGraph_t g;
     CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream);
-    cudaError_t le = launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
+    cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
+                         ? gen_launch(c->gen_fn, n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream)
+                         : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
     if (ce != cudaSuccess) return fail(c, -2, "graph capture: %s", cudaGetErrorString(ce));
@@ -463,11 +506,19 @@ int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_op
   c->net = n;
   c->opt = *opt;
   c->has_net = true;
+  c->gen_fn = nullptr;
+  c->gen_block = 0;
   if (c->graph) {
     cudaGraphExecDestroy(c->graph);
     c->graph = nullptr;
   }
-  if (!c->launch_forced) default_launch(c);
+  if (!c->launch_forced) {
+    // the network-specialized kernel is the default; a compile failure is an error
+    default_launch(c);
+    if (default_specialized_launch(c) != 0) return -2;
+  } else if (c->launch.variant == PFCHEM_KERNEL_SPECIALIZED) {
+    if (ensure_gen(c, c->launch.block_threads) < 1) return -2;
+  }
   return 0;
 }
 
@@ -531,11 +582,22 @@ int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
     return fail(c, -1, "block_threads must be a multiple of 32 in [32, 256]");
   if (l->refill_min_idle < 1 || l->refill_min_idle > 32) return fail(c, -1, "refill_min_idle must be in [1, 32]");
   if (l->blocks_per_sm < 1) return fail(c, -1, "blocks_per_sm must be >= 1");
+  if (l->variant != PFCHEM_KERNEL_SPECIALIZED && l->variant != PFCHEM_KERNEL_GENERIC)
+    return fail(c, -1, "unknown kernel variant %d", l->variant);
   if (c->has_net) {
-    const size_t shm = (size_t)c->net.N * c->net.N * l->block_threads * sizeof(double);
-    if (shm > 227 * 1024) return fail(c, -1, "block_threads %d needs %zu bytes of shared memory", l->block_threads, shm);
-    int nb = max_active_blocks(c->net, l->block_threads);
-    if (nb < 1) return fail(c, -1, "mapping does not fit on an SM");
+    if (l->variant == PFCHEM_KERNEL_SPECIALIZED) {
+      if (gen_shared_bytes(c->net, l->block_threads) > 227 * 1024)
+        return fail(c, -1, "block_threads %d needs too much shared memory", l->block_threads);
+      int nb = ensure_gen(c, l->block_threads);
+      if (nb < 1) return -2;
+      if (l->blocks_per_sm > nb) return fail(c, -1, "at most %d blocks of %d threads fit on an SM", nb, l->block_threads);
+    } else {
+      const size_t shm = (size_t)c->net.N * c->net.N * l->block_threads * sizeof(double);
+      if (shm > 227 * 1024) return fail(c, -1, "block_threads %d needs %zu bytes of shared memory", l->block_threads, shm);
+      int nb = max_active_blocks(c->net, l->block_threads);
+      if (nb < 1) return fail(c, -1, "mapping does not fit on an SM");
+      if (l->blocks_per_sm > nb) return fail(c, -1, "at most %d blocks of %d threads fit on an SM", nb, l->block_threads);
+    }
   }
   c->launch = *l;
   c->launch_forced = true;
@@ -571,17 +633,16 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
     CUDA_TRY(c, cudaMemcpyAsync(x.save, x.p, x.bytes, cudaMemcpyDeviceToDevice, c->stream));
   }
   const int blocks[] = {32, 64, 128};
-  const int refills[] = {1, 8, 16, 32};
+  const int refills[] = {1, 4, 8, 16, 32};
   double best = 1e30;
   pfchem_launch best_l = c->launch;
   int rc = 0;
   for (int b : blocks) {
-    const size_t shm = (size_t)n.N * n.N * b * sizeof(double);
-    if (shm > 227 * 1024) continue;
-    int nb = max_active_blocks(n, b);
+    if (gen_shared_bytes(n, b) > 227 * 1024) continue;
+    int nb = ensure_gen(c, b);
     if (nb < 1) continue;
     for (int r : refills) {
-      pfchem_launch l{b, nb, r, 0};
+      pfchem_launch l{b, nb, r, PFCHEM_KERNEL_SPECIALIZED};
       c->launch = l;
       rc = pfchem_react_batch(c, dt, cl);
       if (rc < 0) break;
@@ -602,7 +663,32 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   if (rc < 0) return rc;
   c->launch = best_l;
   c->launch_forced = true;
+  if (best_l.variant == PFCHEM_KERNEL_SPECIALIZED && ensure_gen(c, best_l.block_threads) < 1) return -2;
   return 0;
+}
+
+int pfchem_check_specialized(const pfchem_network *net, const pfchem_options *opt, int block_threads, char *log,
+                             size_t loglen) {
+  pfchem_ctx tmp;
+  DevNet n;
+  int r = build_devnet(&tmp, net, opt, n);
+  if (r) {
+    if (log && loglen) snprintf(log, loglen, "%s", tmp.err);
+    return r;
+  }
+  const std::string src = generate_source(n, block_threads);
+  nvrtcProgram prog;
+  if (nvrtcCreateProgram(&prog, src.c_str(), "pfchem_gen.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) return -2;
+  const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--fmad=true",
+                        "--ptxas-options=-v"};
+  nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
+  size_t ls = 0;
+  nvrtcGetProgramLogSize(prog, &ls);
+  std::string lg(ls, '\0');
+  nvrtcGetProgramLog(prog, &lg[0]);
+  nvrtcDestroyProgram(&prog);
+  if (log && loglen) snprintf(log, loglen, "%s", lg.c_str());
+  return rc == NVRTC_SUCCESS ? 0 : -2;
 }
 
 }  // extern "C"

@@ -62,30 +62,41 @@ struct DevNet {
 };
 
 // Per-call pointers (device memory, SoA, field(i, cell) at [i * ncells + cell]).
-struct CellArgs {
-  int64_t ncells;
-  double dt;
-  const double *temp, *sat, *den, *por, *vol, *rho_s;
-  const int32_t *active;
-  const double *total;
-  int64_t total_stride_cell;  // 1 for SoA; ncomp for RTReact's interleaved tran_xx
-  int64_t total_stride_comp;  // ncells for SoA; 1 for interleaved
-  double *pri_molal, *ionic, *lnaw, *vf, *area, *sorb, *ixref, *srfree;
-  double *total_out, *rate, *sec_molal;
-  int32_t *iters, *status;
-  const double *alt_guess;
-  double *interleaved_out;  // RTReact layout write-back of the free ions, or null
-};
+// The field lists are macros so that the network-specialized kernels, which
+// are compiled at run time, declare byte-identical structures.
+#define PFCHEM_CELLARGS_FIELDS                                                          \
+  int64_t ncells;                                                                     \
+  double dt;                                                                          \
+  const double *temp, *sat, *den, *por, *vol, *rho_s;                                 \
+  const int32_t *active;                                                              \
+  const double *total;                                                                \
+  int64_t total_stride_cell; /* 1 for SoA; ncomp for RTReact's interleaved tran_xx */ \
+  int64_t total_stride_comp; /* ncells for SoA; 1 for interleaved */                  \
+  double *pri_molal, *ionic, *lnaw, *vf, *area, *sorb, *ixref, *srfree;               \
+  double *total_out, *rate, *sec_molal;                                               \
+  int32_t *iters, *status;                                                            \
+  const double *alt_guess;                                                            \
+  double *interleaved_out; /* RTReact layout write-back of the free ions, or null */
 
 // Work queue and statistics: global memory the solve kernel uses besides its
 // inputs and outputs.
-struct Scratch {
-  unsigned long long next_cell;  // work-queue head
-  unsigned long long sum_iter;
-  unsigned long long alt_used;
-  unsigned int max_iter;
+#define PFCHEM_SCRATCH_FIELDS                            \
+  unsigned long long next_cell; /* work-queue head */ \
+  unsigned long long sum_iter;                        \
+  unsigned long long alt_used;                        \
+  unsigned int max_iter;                              \
   unsigned int nonconverged;
+
+struct CellArgs {
+  PFCHEM_CELLARGS_FIELDS
 };
+
+struct Scratch {
+  PFCHEM_SCRATCH_FIELDS
+};
+
+#define PFCHEM_STR_(...) #__VA_ARGS__
+#define PFCHEM_STR(...) PFCHEM_STR_(__VA_ARGS__)
 
 struct LaunchCfg {
   int refill_min_idle;

@@ -63,6 +63,8 @@ def load(build_if_missing=True):
     l.pfchem_get_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_set_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_autotune.argtypes = [vp, C.c_double, C.POINTER(abi.Cells)]
+    l.pfchem_check_specialized.argtypes = [C.POINTER(abi.Network), C.POINTER(abi.Options), C.c_int, C.c_char_p,
+                                           C.c_size_t]
     _lib = l
     return l
 
@@ -132,8 +134,8 @@ class ReactionStep:
         self._lib.pfchem_get_launch(self._ctx, C.byref(l))
         return l
 
-    def set_launch(self, block_threads, blocks_per_sm, refill_min_idle):
-        l = abi.Launch(block_threads, blocks_per_sm, refill_min_idle, 0)
+    def set_launch(self, block_threads, blocks_per_sm, refill_min_idle, variant=abi.KERNEL_SPECIALIZED):
+        l = abi.Launch(block_threads, blocks_per_sm, refill_min_idle, variant)
         self._check(self._lib.pfchem_set_launch(self._ctx, C.byref(l)), "pfchem_set_launch")
 
     def autotune(self, cells, dt):

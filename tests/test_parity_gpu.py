@@ -206,3 +206,32 @@ def test_calcite_grid_full_size_sampled(oracle):
     sub.sec_molal = np.zeros(net.Nc * len(idx))
     oracle.react(net.as_struct(), opt, dt, sub, 0, 8)
     assert_parity(net, g.subset(idx, net), sub)
+
+
+@pytest.mark.parametrize("kind", ["calcite", "synthetic"])
+def test_generic_table_driven_kernel(oracle, kind):
+    """The library's built-in table-driven kernel (used when the specialized
+    kernel is not selected, and by the allocation-free entry point)."""
+    if kind == "calcite":
+        net, opt, cells, dt = workloads.calcite_cells(2048, seed=12, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(2048, seed=13)
+    ref = cells.copy()
+    ref.sec_molal = np.zeros(max(net.Nc, 1) * cells.ncells)
+    oracle.react(net.as_struct(), opt, dt, ref, 0, 8)
+    step = ReactionStep(net, opt)
+    step.set_launch(64, 1, 8, variant=abi.KERNEL_GENERIC)
+    gpu = cells.copy()
+    gpu.sec_molal = np.zeros(max(net.Nc, 1) * cells.ncells)
+    d = gpu.to_device()
+    step.react(d, dt)
+    g = d.to_host()
+    ok = (ref.status == 0) & (g.status == 0)
+    assert ok.mean() > 0.99
+    assert_parity(net, g, ref, mask=ok)
+
+
+def test_specialized_kernel_is_default():
+    net, opt, cells, dt = workloads.calcite_cells(16, seed=14)
+    step = ReactionStep(net, opt)
+    assert step.launch().variant == abi.KERNEL_SPECIALIZED
