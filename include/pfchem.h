@@ -270,6 +270,54 @@ int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
  * restored after every trial) and keeps the fastest. */
 int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
 
+/* ---------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference).  A BF16 MLP
+ * 16 -> 256 -> 256 -> 256 -> 12 (GELU, FP32 accumulate) maps per-cell features
+ * (signed-log conserved totals, pH proxy, T, log ionic strength) to the
+ * step's log-molalities.  It is trained on the GPU with the library's own
+ * tensor-core kernels on solves produced by pfchem_react_batch itself; when
+ * enabled, pfchem_react_batch predicts an alternative guess for every cell
+ * and FP64 Newton starts from it only where its first residual is no worse
+ * than the previous-step guess's.  All pointers are device pointers. */
+#define PFCHEM_SURROGATE_FEATURES 16
+typedef struct pfchem_surrogate_cfg {
+  int32_t epochs;       /* passes over the samples                    */
+  int32_t batch;        /* rows per optimiser step                    */
+  float lr;             /* AdamW learning rate                        */
+  float weight_decay;   /* AdamW decoupled weight decay               */
+  uint64_t seed;        /* weight initialisation and batch order      */
+} pfchem_surrogate_cfg;
+typedef struct pfchem_surrogate_report {
+  int64_t samples;
+  int64_t steps;
+  float first_loss;     /* mean squared error (standardised units), first step */
+  float final_loss;     /* mean over the last epoch's steps           */
+  double train_ms;      /* wall time of the fit                       */
+} pfchem_surrogate_report;
+/* Features of each cell of `cells` (device) into X [ncells][16] (float). */
+int pfchem_surrogate_features(pfchem_ctx *ctx, pfchem_cells *cells, float *X);
+/* Trains the context's network on M samples: X [M][16] features taken before
+ * the step, molal (SoA [naqcomp][M], double) the converged free-ion
+ * molalities of those steps.  Pass converged samples only. */
+int pfchem_surrogate_fit(pfchem_ctx *ctx, const float *X, const double *molal, int64_t M,
+                         const pfchem_surrogate_cfg *cfg, pfchem_surrogate_report *report);
+/* The network's prediction for each cell of `cells` (device) into guess
+ * (SoA [naqcomp][ncells] free-ion molalities, device). */
+int pfchem_surrogate_predict(pfchem_ctx *ctx, pfchem_cells *cells, double *guess);
+/* 1 = predict the alternative guess inside pfchem_react_batch (needs a fit). */
+int pfchem_surrogate_enable(pfchem_ctx *ctx, int on);
+/* Loss and gradients of the current weights on M samples, without updating
+ * them (grad_host[nparam] on the host; returns nparam, or < 0). */
+int64_t pfchem_surrogate_gradients(pfchem_ctx *ctx, const float *X, const double *molal, int64_t M,
+                                   float *grad_host, float *loss_host);
+/* Gets (set = 0) or sets (set = 1) the FP32 master weights, layer by layer
+ * W (in x out, row-major) then b; returns the parameter count. */
+int64_t pfchem_surrogate_params(pfchem_ctx *ctx, float *host, int set);
+/* Gets or sets the standardisation: features (mean, 1/std) [16] each,
+ * targets ln m (mean, std) [naqcomp] each. */
+int pfchem_surrogate_normalization(pfchem_ctx *ctx, float *feat_mean, float *feat_inv_std, float *tgt_mean,
+                                   float *tgt_std, int set);
+
 /* Generates and compiles (NVRTC, sm_103a) the network-specialized solve
  * kernel for `net`/`opt` with `block_threads` threads per block, without
  * loading it; needs no GPU.  Returns 0 or < 0 with the compiler log in

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpfchem.so")
 PROBE = os.path.join(OUT, "libpfchem_probe.so")
-SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu", "pfchem_codegen.cu"]
+SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu", "pfchem_codegen.cu", "pfchem_mlp.cu"]
 PROBE_SOURCES = ["fp64_peak.cu"]
 HEADERS = ["pfchem_device.cuh", os.path.join("..", "..", "include", "pfchem.h")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",

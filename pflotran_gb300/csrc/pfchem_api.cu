@@ -13,6 +13,7 @@
 #include <cstring>
 #include <string>
 #include <vector>
+#include <random>
 #include <nvrtc.h>
 
 #include "../../include/pfchem.h"
@@ -29,6 +30,24 @@ size_t gen_shared_bytes(const DevNet &n, int block);
 std::string generate_source(const DevNet &n, int block);
 cudaError_t gen_launch(void *fn, const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
                        cudaStream_t st);
+struct Surrogate;
+Surrogate *surrogate_create(int N, uint64_t seed, std::string *err);
+void surrogate_destroy(Surrogate *s);
+size_t surrogate_nparam(const Surrogate *s);
+cudaError_t surrogate_features(const DevNet &n, const CellArgs &a, float *X, cudaStream_t st);
+void surrogate_set_norm(Surrogate *s, const float *fmu, const float *fisd, const float *tmu, const float *tsd);
+float surrogate_train_step(Surrogate *s, const float *X, const float *T, long long rows, float lr, float wd,
+                           cudaStream_t st, bool sync, cudaError_t *err);
+cudaError_t surrogate_gradients(Surrogate *s, const float *X, const float *T, long long rows, float *grad_host,
+                                float *loss_host, cudaStream_t st);
+cudaError_t surrogate_get_params(Surrogate *s, float *host);
+cudaError_t surrogate_set_params(Surrogate *s, const float *host);
+cudaError_t surrogate_prepare(Surrogate *s, long long ncells);
+double *surrogate_guess_buffer(Surrogate *s);
+cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st);
+cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, float *T, cudaStream_t st);
+void surrogate_mark_trained(Surrogate *s, bool t);
+bool surrogate_trained(const Surrogate *s);
 }  // namespace pfchem
 
 using namespace pfchem;
@@ -57,6 +76,9 @@ struct pfchem_ctx {
   pfchem_launch graph_launch{};
   void *gen_fn = nullptr;  // specialized kernel for gen_block threads per block
   int gen_block = 0;
+  Surrogate *sur = nullptr;  // learned warm start
+  bool sur_on = false;
+  float norm[2 * 16 + 2 * PFCHEM_MAX_PRI] = {};  // host copy of the standardisation
   char err[2048] = {0};
 };
 
@@ -329,11 +351,18 @@ CellArgs device_args(const pfchem_cells *cl, double dt) {
   return a;
 }
 
-int run_solve(pfchem_ctx *c, const CellArgs &a) {
+int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
   const DevNet &n = c->net;
-  if (a.ncells == 0) {
+  if (a_in.ncells == 0) {
     c->stats = pfchem_stats{};
     return 0;
+  }
+  CellArgs a = a_in;
+  const bool predict = c->sur && c->sur_on && surrogate_trained(c->sur) && !a.alt_guess;
+  if (predict) {
+    cudaError_t pe = surrogate_prepare(c->sur, a.ncells);
+    if (pe != cudaSuccess) return fail(c, -2, "surrogate buffers: %s", cudaGetErrorString(pe));
+    a.alt_guess = surrogate_guess_buffer(c->sur);
   }
   const pfchem_launch &L = c->launch;
   const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
@@ -348,10 +377,12 @@ int run_solve(pfchem_ctx *c, const CellArgs &a) {
     cudaGraph_t g;
     CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream);
+    cudaError_t pe = predict ? surrogate_predict(c->sur, n, a, c->stream) : cudaSuccess;
     cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
                          ? gen_launch(c->gen_fn, n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream)
                          : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
+    if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
     if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
     if (ce != cudaSuccess) return fail(c, -2, "graph capture: %s", cudaGetErrorString(ce));
     cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
@@ -486,6 +517,7 @@ void pfchem_destroy(pfchem_ctx *c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->graph) cudaGraphExecDestroy(c->graph);
+  if (c->sur) surrogate_destroy(c->sur);
   for (auto &b : c->stage)
     if (b.ptr) cudaFree(b.ptr);
   if (c->scratch) cudaFree(c->scratch);
@@ -664,6 +696,216 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   c->launch = best_l;
   c->launch_forced = true;
   if (best_l.variant == PFCHEM_KERNEL_SPECIALIZED && ensure_gen(c, best_l.block_threads) < 1) return -2;
+  return 0;
+}
+
+static int need_surrogate(pfchem_ctx *c, uint64_t seed) {
+  if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
+  if (c->sur) return 0;
+  std::string e;
+  c->sur = surrogate_create(c->net.N, seed, &e);
+  if (!c->sur) return fail(c, -2, "surrogate: %s", e.c_str());
+  return 0;
+}
+
+int pfchem_surrogate_features(pfchem_ctx *c, pfchem_cells *cl, float *X) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device || !X) return fail(c, -1, "device pointers required");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  CUDA_TRY(c, surrogate_features(c->net, a, X, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+// Standardisation from up to 65536 samples copied to the host.
+static int fit_norm(pfchem_ctx *c, const float *X, const double *molal, int64_t M) {
+  const int N = c->net.N;
+  const int64_t S = std::min<int64_t>(M, 65536);
+  std::vector<float> xs(S * 16);
+  std::vector<double> ms((size_t)N * S);
+  CUDA_TRY(c, cudaMemcpy(xs.data(), X, S * 16 * sizeof(float), cudaMemcpyDeviceToHost));
+  for (int j = 0; j < N; ++j)
+    CUDA_TRY(c, cudaMemcpy(ms.data() + (size_t)j * S, molal + (size_t)j * M, S * sizeof(double),
+                           cudaMemcpyDeviceToHost));
+  float fmu[16], fisd[16], tmu[PFCHEM_MAX_PRI], tsd[PFCHEM_MAX_PRI];
+  for (int f = 0; f < 16; ++f) {
+    double s = 0, s2 = 0;
+    for (int64_t r = 0; r < S; ++r) {
+      s += xs[r * 16 + f];
+      s2 += (double)xs[r * 16 + f] * xs[r * 16 + f];
+    }
+    const double mu = s / S, var = std::max(s2 / S - mu * mu, 0.0);
+    fmu[f] = (float)mu;
+    fisd[f] = var > 1e-12 ? (float)(1.0 / std::sqrt(var)) : 1.0f;
+  }
+  for (int j = 0; j < N; ++j) {
+    double s = 0, s2 = 0;
+    for (int64_t r = 0; r < S; ++r) {
+      const double v = std::log(ms[(size_t)j * S + r]);
+      s += v;
+      s2 += v * v;
+    }
+    const double mu = s / S, var = std::max(s2 / S - mu * mu, 0.0);
+    tmu[j] = (float)mu;
+    tsd[j] = var > 1e-12 ? (float)std::sqrt(var) : 1.0f;
+  }
+  surrogate_set_norm(c->sur, fmu, fisd, tmu, tsd);
+  std::memcpy(c->norm, fmu, sizeof(fmu));
+  std::memcpy(c->norm + 16, fisd, sizeof(fisd));
+  std::memcpy(c->norm + 32, tmu, sizeof(float) * PFCHEM_MAX_PRI);
+  std::memcpy(c->norm + 32 + PFCHEM_MAX_PRI, tsd, sizeof(float) * PFCHEM_MAX_PRI);
+  return 0;
+}
+
+int pfchem_surrogate_fit(pfchem_ctx *c, const float *X, const double *molal, int64_t M,
+                         const pfchem_surrogate_cfg *cfg, pfchem_surrogate_report *rep) {
+  if (!c || !X || !molal || !cfg) return -1;
+  if (M < 1) return fail(c, -1, "no samples");
+  if (cfg->batch < 1 || cfg->epochs < 1) return fail(c, -1, "batch and epochs must be >= 1");
+  cudaSetDevice(c->device);
+  int e = need_surrogate(c, cfg->seed);
+  if (e) return e;
+  if ((e = fit_norm(c, X, molal, M))) return e;
+  const int N = c->net.N;
+  float *T = nullptr;
+  CUDA_TRY(c, cudaMalloc(&T, (size_t)M * N * sizeof(float)));
+  cudaError_t ce = surrogate_targets(c->sur, molal, M, T, c->stream);
+  if (ce != cudaSuccess) {
+    cudaFree(T);
+    return fail(c, -2, "targets: %s", cudaGetErrorString(ce));
+  }
+  cudaEvent_t t0, t1;
+  cudaEventCreate(&t0);
+  cudaEventCreate(&t1);
+  cudaEventRecord(t0, c->stream);
+  const int64_t B = std::min<int64_t>(cfg->batch, M);
+  const int64_t nb = M / B;
+  std::vector<int64_t> order(nb);
+  for (int64_t i = 0; i < nb; ++i) order[i] = i;
+  std::mt19937_64 rng(cfg->seed ^ 0x9e3779b97f4a7c15ULL);
+  float first = NAN, last_sum = 0.f;
+  int64_t last_n = 0, steps = 0;
+  for (int ep = 0; ep < cfg->epochs; ++ep) {
+    std::shuffle(order.begin(), order.end(), rng);
+    const bool last_epoch = ep == cfg->epochs - 1;
+    for (int64_t i = 0; i < nb; ++i) {
+      const int64_t r0 = order[i] * B;
+      const bool sync = (steps == 0) || (last_epoch && (i % 16 == 0));
+      // cosine decay of the learning rate over the whole fit
+      const double frac = (double)steps / (double)std::max<int64_t>(1, (int64_t)cfg->epochs * nb);
+      const float lr = (float)(cfg->lr * (0.02 + 0.98 * 0.5 * (1.0 + std::cos(3.14159265358979 * frac))));
+      float l = surrogate_train_step(c->sur, X + r0 * 16, T + r0 * N, B, lr, cfg->weight_decay, c->stream,
+                                     sync, &ce);
+      if (ce != cudaSuccess) break;
+      if (steps == 0) first = l / (float)(B * N);
+      if (sync && last_epoch) {
+        last_sum += l / (float)(B * N);
+        last_n += 1;
+      }
+      ++steps;
+    }
+    if (ce != cudaSuccess) break;
+  }
+  cudaEventRecord(t1, c->stream);
+  cudaStreamSynchronize(c->stream);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, t0, t1);
+  cudaEventDestroy(t0);
+  cudaEventDestroy(t1);
+  cudaFree(T);
+  if (ce != cudaSuccess) return fail(c, -2, "training: %s", cudaGetErrorString(ce));
+  surrogate_mark_trained(c->sur, true);
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  if (rep) {
+    rep->samples = nb * B;
+    rep->steps = steps;
+    rep->first_loss = first;
+    rep->final_loss = last_n ? last_sum / last_n : NAN;
+    rep->train_ms = ms;
+  }
+  return 0;
+}
+
+int pfchem_surrogate_predict(pfchem_ctx *c, pfchem_cells *cl, double *guess) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device || !guess) return fail(c, -1, "device pointers required");
+  if (!c->sur || !surrogate_trained(c->sur)) return fail(c, -1, "the surrogate has not been trained");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  CUDA_TRY(c, surrogate_prepare(c->sur, a.ncells));
+  CUDA_TRY(c, surrogate_predict(c->sur, c->net, a, c->stream));
+  CUDA_TRY(c, cudaMemcpyAsync(guess, surrogate_guess_buffer(c->sur), (size_t)c->net.N * a.ncells * sizeof(double),
+                              cudaMemcpyDeviceToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int pfchem_surrogate_enable(pfchem_ctx *c, int on) {
+  if (!c) return -1;
+  if (on && (!c->sur || !surrogate_trained(c->sur))) return fail(c, -1, "the surrogate has not been trained");
+  c->sur_on = on != 0;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  return 0;
+}
+
+int64_t pfchem_surrogate_gradients(pfchem_ctx *c, const float *X, const double *molal, int64_t M, float *grad_host,
+                                   float *loss_host) {
+  if (!c || !X || !molal || !grad_host || !loss_host) return -1;
+  cudaSetDevice(c->device);
+  int e = need_surrogate(c, 1);
+  if (e) return e;
+  const int N = c->net.N;
+  float *T = nullptr;
+  CUDA_TRY(c, cudaMalloc(&T, (size_t)M * N * sizeof(float)));
+  cudaError_t ce = surrogate_targets(c->sur, molal, M, T, c->stream);
+  if (ce == cudaSuccess) ce = surrogate_gradients(c->sur, X, T, M, grad_host, loss_host, c->stream);
+  cudaFree(T);
+  if (ce != cudaSuccess) return fail(c, -2, "gradients: %s", cudaGetErrorString(ce));
+  return (int64_t)surrogate_nparam(c->sur);
+}
+
+int64_t pfchem_surrogate_params(pfchem_ctx *c, float *host, int set) {
+  if (!c) return -1;
+  cudaSetDevice(c->device);
+  int e = need_surrogate(c, 1);
+  if (e) return e;
+  if (host) {
+    cudaError_t ce = set ? surrogate_set_params(c->sur, host) : surrogate_get_params(c->sur, host);
+    if (ce != cudaSuccess) return fail(c, -2, "params: %s", cudaGetErrorString(ce));
+    if (set) surrogate_mark_trained(c->sur, true);
+  }
+  return (int64_t)surrogate_nparam(c->sur);
+}
+
+int pfchem_surrogate_normalization(pfchem_ctx *c, float *fmu, float *fisd, float *tmu, float *tsd, int set) {
+  if (!c) return -1;
+  cudaSetDevice(c->device);
+  int e = need_surrogate(c, 1);
+  if (e) return e;
+  const int N = c->net.N;
+  if (set) {
+    surrogate_set_norm(c->sur, fmu, fisd, tmu, tsd);
+    std::memcpy(c->norm, fmu, 16 * sizeof(float));
+    std::memcpy(c->norm + 16, fisd, 16 * sizeof(float));
+    std::memcpy(c->norm + 32, tmu, N * sizeof(float));
+    std::memcpy(c->norm + 32 + PFCHEM_MAX_PRI, tsd, N * sizeof(float));
+  } else {
+    std::memcpy(fmu, c->norm, 16 * sizeof(float));
+    std::memcpy(fisd, c->norm + 16, 16 * sizeof(float));
+    std::memcpy(tmu, c->norm + 32, N * sizeof(float));
+    std::memcpy(tsd, c->norm + 32 + PFCHEM_MAX_PRI, N * sizeof(float));
+  }
   return 0;
 }
 

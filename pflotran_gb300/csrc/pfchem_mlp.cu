@@ -1,0 +1,550 @@
+// pfchem_mlp.cu -- learned warm start for the per-cell Newton solve.
+//
+// A 16 -> 256 -> 256 -> 256 -> 12 multilayer perceptron (GELU) maps per-cell
+// features of the step -- the signed-log totals that the step conserves
+// (aqueous plus sorbed, per litre of pore water), a pH proxy, temperature and
+// the ionic strength of the previous state -- to the 12 log-molalities of the
+// step's solution.  Weights and activations are BF16, products accumulate in
+// FP32 on the tensor cores (mma.sync m16n8k16), and it is trained here, with
+// these kernels, on solves produced by the FP64 Newton kernel itself.  FP64
+// Newton always finishes every cell: the prediction enters as the solve's
+// alternative guess, taken per cell only if its first residual is no worse
+// than the previous-step guess's.
+//
+// Kernels: one tiled BF16 GEMM (operands read through arbitrary row/column
+// strides, so the same kernel serves X W, dY W^T and X^T dY) with fused
+// bias + GELU epilogues; GELU backward; bias gradients; the MSE loss and its
+// gradient; AdamW on FP32 master weights (refreshing the BF16 copies); the
+// feature and output transforms.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <random>
+#include <string>
+#include <vector>
+
+#include "pfchem_device.cuh"
+
+namespace pfchem {
+
+constexpr int kFeat = 16;    // input features
+constexpr int kHidden = 256;  // hidden width
+constexpr int kOut = PFCHEM_MAX_PRI;  // outputs (the first N used)
+constexpr int kLayers = 4;
+
+namespace {
+
+using bf16 = __nv_bfloat16;
+
+__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float x) {
+  const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+  const float pdf = 0.39894228040143268f * expf(-0.5f * x * x);
+  return cdf + x * pdf;
+}
+
+__device__ __forceinline__ void mma16816(float *c, const uint32_t *a, const uint32_t *b) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};\n"
+      : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// C(m, n) = sum_k A(m, k) B(k, n), A(m, k) = A[m*sam + k*sak], B(k, n) = B[k*sbk + n*sbn].
+// Epilogues: kEpiAct: Cf = acc + bias (FP32), Cb = act(acc + bias) (BF16);
+//            kEpiF32: Cf = acc (+ bias); kEpiAccF32: Cf += acc (FP32 accumulate, no bias).
+enum { kEpiAct = 0, kEpiF32 = 1 };
+constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
+
+template <int EPI>
+__global__ void __launch_bounds__(128) gemm_bf16(const bf16 *__restrict__ A, long long sam, long long sak,
+                                                  const bf16 *__restrict__ B, long long sbk, long long sbn, int M,
+                                                  int N, int K, const float *__restrict__ bias, float *Cf, bf16 *Cb,
+                                                  int ldc, int act) {
+  __shared__ __align__(16) bf16 As[BM][BK + PAD];
+  __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int wm = warp >> 1, wn = warp & 1;
+  const int g = lane >> 2, t = lane & 3;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  float acc[2][4][4];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
+  const bf16 zero = __float2bfloat16(0.f);
+  for (int k0 = 0; k0 < K; k0 += BK) {
+    for (int e = tid; e < BM * BK; e += 128) {
+      const int mm = e / BK, kk = e % BK;
+      const int gm = m0 + mm, gk = k0 + kk;
+      As[mm][kk] = (gm < M && gk < K) ? A[(long long)gm * sam + (long long)gk * sak] : zero;
+    }
+    for (int e = tid; e < BN * BK; e += 128) {
+      const int nn = e / BK, kk = e % BK;
+      const int gn = n0 + nn, gk = k0 + kk;
+      Bs[nn][kk] = (gn < N && gk < K) ? B[(long long)gk * sbk + (long long)gn * sbn] : zero;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int ks = 0; ks < BK; ks += 16) {
+      uint32_t a[2][4], b[4][2];
+#pragma unroll
+      for (int i = 0; i < 2; ++i) {
+        const int r = wm * 32 + i * 16 + g;
+        a[i][0] = *reinterpret_cast<const uint32_t *>(&As[r][ks + 2 * t]);
+        a[i][1] = *reinterpret_cast<const uint32_t *>(&As[r + 8][ks + 2 * t]);
+        a[i][2] = *reinterpret_cast<const uint32_t *>(&As[r][ks + 2 * t + 8]);
+        a[i][3] = *reinterpret_cast<const uint32_t *>(&As[r + 8][ks + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int c = wn * 32 + j * 8 + g;
+        b[j][0] = *reinterpret_cast<const uint32_t *>(&Bs[c][ks + 2 * t]);
+        b[j][1] = *reinterpret_cast<const uint32_t *>(&Bs[c][ks + 2 * t + 8]);
+      }
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) mma16816(acc[i][j], a[i], b[j]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int r = m0 + wm * 32 + i * 16 + g + (q >= 2 ? 8 : 0);
+        const int c = n0 + wn * 32 + j * 8 + 2 * t + (q & 1);
+        if (r < M && c < N) {
+          float z = acc[i][j][q] + (bias ? bias[c] : 0.f);
+          const long long o = (long long)r * ldc + c;
+          if (EPI == kEpiAct) {
+            if (Cf) Cf[o] = z;
+            Cb[o] = __float2bfloat16(act ? gelu(z) : z);
+          } else {
+            Cf[o] = z;
+          }
+        }
+      }
+}
+
+// dZ = dH * GELU'(Z), dH given in FP32; output BF16 (GEMM operand) and FP32 kept
+__global__ void gelu_backward(const float *__restrict__ dH, const float *__restrict__ Z, bf16 *dZb, float *dZf,
+                              long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float v = dH[i] * gelu_grad(Z[i]);
+  dZb[i] = __float2bfloat16(v);
+  if (dZf) dZf[i] = v;
+}
+
+// db[c] = sum_r dZ[r, c] (rows split over blockIdx.y, atomics into db)
+__global__ void bias_grad(const float *__restrict__ dZ, float *db, int M, int N) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  const int rows_per = (M + gridDim.y - 1) / gridDim.y;
+  const int r0 = blockIdx.y * rows_per, r1 = min(M, r0 + rows_per);
+  float s = 0.f;
+  for (int r = r0; r < r1; ++r) s += dZ[(long long)r * N + c];
+  atomicAdd(&db[c], s);
+}
+
+// MSE over the first `nout` outputs: dY = 2 (Y - T) / (M nout), loss sum
+__global__ void mse_loss(const float *__restrict__ Y, const float *__restrict__ T, float *dY, bf16 *dYb, int M,
+                         int ldy, int nout, float *loss) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float l = 0.f;
+  if (i < (long long)M * ldy) {
+    const int c = (int)(i % ldy);
+    float d = 0.f;
+    if (c < nout) {
+      const long long r = i / ldy;
+      d = Y[i] - T[r * nout + c];
+      l = d * d;
+    }
+    const float gval = 2.f * d / ((float)M * nout);
+    dY[i] = gval;
+    dYb[i] = __float2bfloat16(gval);
+  }
+  for (int o = 16; o > 0; o >>= 1) l += __shfl_xor_sync(0xffffffffu, l, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(loss, l);
+}
+
+__global__ void adamw(float *w, bf16 *wb, const float *g, float *m, float *v, long long n, float lr, float b1,
+                      float b2, float eps, float wd, float bc1, float bc2) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  float wi = w[i] * (1.f - lr * wd);
+  wi -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  w[i] = wi;
+  if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+__global__ void to_bf16(const float *x, bf16 *y, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) y[i] = __float2bfloat16(x[i]);
+}
+
+// Per-cell features (raw, before standardisation), row-major [cell][kFeat].
+__global__ void cell_features(const CellArgs a, int N, int sorb, float *X) {
+  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (cell >= a.ncells) return;
+  const long long nc = a.ncells;
+  const double por = a.por[cell], sat = a.sat[cell], vol = a.vol[cell];
+  const double psv = por * sat * 1000.0 * vol;
+  float *x = X + cell * kFeat;
+  for (int j = 0; j < kFeat; ++j) x[j] = 0.f;
+  for (int j = 0; j < N; ++j) {
+    double acc = psv * a.total[j * a.total_stride_comp + cell * a.total_stride_cell];
+    if (sorb) acc += vol * a.sorb[j * nc + cell];
+    x[j] = (float)asinh(acc / psv * 1e12);  // signed log of the conserved total [mol/L pore water]
+  }
+  x[12] = (float)(-log10(a.pri_molal[cell]));  // pH proxy: the H+-like first species of the guess
+  x[13] = (float)a.temp[cell];
+  x[14] = (float)log10(fmax(a.ionic[cell], 1e-30));
+}
+
+__global__ void standardize(const float *X, const float *mu, const float *sd, bf16 *Xb, long long rows, int cols) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  const int c = (int)(i % cols);
+  Xb[i] = __float2bfloat16((X[i] - mu[c]) * sd[c]);
+}
+
+// Predicted log-molalities of rows [r0, r0 + rows) -> alternative guess
+// (SoA [N][ncells]), for the first N outputs.
+__global__ void outputs_to_guess(const float *Y, int ldy, const float *mu, const float *sd, int N, long long rows,
+                                 long long r0, long long ncells, double *guess) {
+  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (r >= rows) return;
+  for (int j = 0; j < N; ++j) {
+    const double lm = (double)mu[j] + (double)sd[j] * (double)Y[r * ldy + j];
+    guess[j * ncells + r0 + r] = exp(fmin(fmax(lm, -700.0), 700.0));
+  }
+}
+
+// Targets: converged molalities (SoA [N][M], double) -> standardised ln m ([M][N], float)
+__global__ void targets_from_molal(const double *molal, long long M, int N, const float *mu, const float *sd,
+                                   float *T) {
+  const long long r = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (r >= M) return;
+  for (int j = 0; j < N; ++j) T[r * N + j] = (float)((log(molal[j * M + r]) - (double)mu[j]) / (double)sd[j]);
+}
+
+unsigned blocks(long long n, int b) { return (unsigned)((n + b - 1) / b); }
+
+template <int EPI>
+void gemm(cudaStream_t st, const bf16 *A, long long sam, long long sak, const bf16 *B, long long sbk, long long sbn,
+          int M, int N, int K, const float *bias, float *Cf, bf16 *Cb, int ldc, int act) {
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
+  gemm_bf16<EPI><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, bias, Cf, Cb, ldc, act);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct Surrogate {
+  int N = 0;           // outputs in use (network's primary species)
+  int dims[kLayers + 1] = {kFeat, kHidden, kHidden, kHidden, kOut};
+  // parameters (FP32 master, BF16 copy), gradients, Adam moments: one buffer each
+  size_t woff[kLayers], boff[kLayers], nparam = 0;
+  float *w = nullptr, *grad = nullptr, *m1 = nullptr, *m2 = nullptr;
+  bf16 *wb = nullptr;
+  float *fmu = nullptr, *fsd = nullptr, *tmu = nullptr, *tsd = nullptr;  // device normalisation
+  bool trained = false;
+  // activations for a batch of `cap` rows (training) or one inference chunk
+  long long cap = 0;
+  bf16 *xb = nullptr, *hb[kLayers] = {}, *db[kLayers] = {};
+  float *z[kLayers] = {}, *dz[kLayers] = {}, *y = nullptr, *dy = nullptr, *tgt = nullptr, *loss = nullptr;
+  float *feat = nullptr;
+  long long feat_cap = 0;
+  double *guess = nullptr;
+  long long guess_cap = 0;
+  int steps = 0;
+};
+
+namespace {
+void free_acts(Surrogate *s) {
+  cudaFree(s->xb);
+  for (int l = 0; l < kLayers; ++l) {
+    cudaFree(s->hb[l]);
+    cudaFree(s->db[l]);
+    cudaFree(s->z[l]);
+    cudaFree(s->dz[l]);
+  }
+  cudaFree(s->y);
+  cudaFree(s->dy);
+  cudaFree(s->tgt);
+  s->xb = nullptr;
+  for (int l = 0; l < kLayers; ++l) s->hb[l] = s->db[l] = nullptr, s->z[l] = s->dz[l] = nullptr;
+  s->y = s->dy = s->tgt = nullptr;
+  s->cap = 0;
+}
+
+cudaError_t ensure_acts(Surrogate *s, long long rows) {
+  if (rows <= s->cap) return cudaSuccess;
+  free_acts(s);
+  cudaError_t e = cudaSuccess;
+  e = cudaMalloc(&s->xb, rows * kFeat * sizeof(bf16));
+  for (int l = 0; l < kLayers && e == cudaSuccess; ++l) {
+    const int w = s->dims[l + 1];
+    e = cudaMalloc(&s->hb[l], rows * w * sizeof(bf16));
+    if (e == cudaSuccess) e = cudaMalloc(&s->db[l], rows * w * sizeof(bf16));
+    if (e == cudaSuccess) e = cudaMalloc(&s->z[l], rows * w * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&s->dz[l], rows * w * sizeof(float));
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&s->y, rows * kOut * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->dy, rows * kOut * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->tgt, rows * kOut * sizeof(float));
+  if (e == cudaSuccess) s->cap = rows;
+  return e;
+}
+
+// forward over `rows` standardised inputs in s->xb; output FP32 in s->y
+void forward(Surrogate *s, long long rows, cudaStream_t st, bool keep) {
+  const bf16 *in = s->xb;
+  for (int l = 0; l < kLayers; ++l) {
+    const int K = s->dims[l], Nn = s->dims[l + 1];
+    const bf16 *W = s->wb + s->woff[l];
+    const float *b = s->w + s->boff[l];
+    if (l < kLayers - 1)
+      gemm<kEpiAct>(st, in, K, 1, W, Nn, 1, (int)rows, Nn, K, b, keep ? s->z[l] : nullptr, s->hb[l], Nn, 1);
+    else
+      gemm<kEpiF32>(st, in, K, 1, W, Nn, 1, (int)rows, Nn, K, b, s->y, nullptr, Nn, 0);
+    in = s->hb[l];
+  }
+}
+
+// loss + gradients for `rows` rows (targets standardised in s->tgt, [rows][N])
+void backward(Surrogate *s, long long rows, cudaStream_t st) {
+  cudaMemsetAsync(s->grad, 0, s->nparam * sizeof(float), st);
+  cudaMemsetAsync(s->loss, 0, sizeof(float), st);
+  // output layer gradient: dY (FP32 in s->dy, BF16 in db[last])
+  mse_loss<<<blocks(rows * kOut, 256), 256, 0, st>>>(s->y, s->tgt, s->dy, s->db[kLayers - 1], (int)rows, kOut,
+                                                       s->N, s->loss);
+  for (int l = kLayers - 1; l >= 0; --l) {
+    const int K = s->dims[l], Nn = s->dims[l + 1];
+    const bf16 *inp = (l == 0) ? s->xb : s->hb[l - 1];
+    const bf16 *dZb = s->db[l];
+    const float *dZf = (l == kLayers - 1) ? s->dy : s->dz[l];
+    // dW[K x N] = inp^T [K x rows] . dZ [rows x N]
+    gemm<kEpiF32>(st, inp, 1, K, dZb, Nn, 1, K, Nn, (int)rows, nullptr, s->grad + s->woff[l], nullptr, Nn, 0);
+    // db = column sums of dZ
+    bias_grad<<<dim3(blocks(Nn, 128), 64), 128, 0, st>>>(dZf, s->grad + s->boff[l], (int)rows, Nn);
+    if (l > 0) {
+      // dH_{l-1} [rows x K] = dZ [rows x N] . W^T, W stored [K x N]
+      const bf16 *W = s->wb + s->woff[l];
+      gemm<kEpiF32>(st, dZb, Nn, 1, W, 1, Nn, (int)rows, K, Nn, nullptr, s->dz[l - 1], nullptr, K, 0);
+      // through the GELU of layer l-1: dZ_{l-1} = dH * GELU'(Z_{l-1}) (in place in dz)
+      gelu_backward<<<blocks(rows * K, 256), 256, 0, st>>>(s->dz[l - 1], s->z[l - 1], s->db[l - 1], s->dz[l - 1],
+                                                           rows * K);
+    }
+  }
+}
+}  // namespace
+
+Surrogate *surrogate_create(int N, uint64_t seed, std::string *err) {
+  Surrogate *s = new Surrogate();
+  s->N = N;
+  size_t off = 0;
+  for (int l = 0; l < kLayers; ++l) {
+    s->woff[l] = off;
+    off += (size_t)s->dims[l] * s->dims[l + 1];
+    s->boff[l] = off;
+    off += s->dims[l + 1];
+  }
+  s->nparam = off;
+  // Kaiming-uniform weights (GELU ~ ReLU gain), zero biases, seeded
+  std::vector<float> h(off, 0.f);
+  std::mt19937_64 rng(seed);
+  for (int l = 0; l < kLayers; ++l) {
+    const double bound = std::sqrt(6.0 / s->dims[l]) * (l == kLayers - 1 ? 0.5 : 1.0);
+    std::uniform_real_distribution<double> U(-bound, bound);
+    for (size_t i = 0; i < (size_t)s->dims[l] * s->dims[l + 1]; ++i) h[s->woff[l] + i] = (float)U(rng);
+  }
+  cudaError_t e = cudaMalloc(&s->w, off * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->grad, off * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->m1, off * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->m2, off * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->wb, off * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&s->fmu, 2 * kFeat * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->tmu, 2 * kOut * sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->loss, sizeof(float));
+  if (e != cudaSuccess) {
+    *err = cudaGetErrorString(e);
+    return nullptr;
+  }
+  s->fsd = s->fmu + kFeat;
+  s->tsd = s->tmu + kOut;
+  cudaMemcpy(s->w, h.data(), off * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemset(s->m1, 0, off * sizeof(float));
+  cudaMemset(s->m2, 0, off * sizeof(float));
+  to_bf16<<<blocks(off, 256), 256>>>(s->w, s->wb, off);
+  std::vector<float> one(2 * kFeat, 0.f);
+  for (int i = 0; i < kFeat; ++i) one[kFeat + i] = 1.f;
+  cudaMemcpy(s->fmu, one.data(), 2 * kFeat * sizeof(float), cudaMemcpyHostToDevice);
+  std::vector<float> onet(2 * kOut, 0.f);
+  for (int i = 0; i < kOut; ++i) onet[kOut + i] = 1.f;
+  cudaMemcpy(s->tmu, onet.data(), 2 * kOut * sizeof(float), cudaMemcpyHostToDevice);
+  cudaDeviceSynchronize();
+  return s;
+}
+
+void surrogate_destroy(Surrogate *s) {
+  if (!s) return;
+  free_acts(s);
+  cudaFree(s->w);
+  cudaFree(s->grad);
+  cudaFree(s->m1);
+  cudaFree(s->m2);
+  cudaFree(s->wb);
+  cudaFree(s->fmu);
+  cudaFree(s->tmu);
+  cudaFree(s->loss);
+  cudaFree(s->feat);
+  cudaFree(s->guess);
+  delete s;
+}
+
+size_t surrogate_nparam(const Surrogate *s) { return s->nparam; }
+
+cudaError_t surrogate_features(const DevNet &n, const CellArgs &a, float *X, cudaStream_t st) {
+  cell_features<<<blocks(a.ncells, 128), 128, 0, st>>>(a, n.N, (n.Nix + n.Nsr) > 0, X);
+  return cudaGetLastError();
+}
+
+// Sets the feature/target standardisation (host arrays: mean[kFeat], inv_std[kFeat], tmean[N], tstd[N]).
+void surrogate_set_norm(Surrogate *s, const float *fmu, const float *fisd, const float *tmu, const float *tsd) {
+  std::vector<float> f(2 * kFeat), t(2 * kOut, 0.f);
+  for (int i = 0; i < kFeat; ++i) {
+    f[i] = fmu[i];
+    f[kFeat + i] = fisd[i];
+  }
+  for (int i = 0; i < kOut; ++i) t[kOut + i] = 1.f;
+  for (int i = 0; i < s->N; ++i) {
+    t[i] = tmu[i];
+    t[kOut + i] = tsd[i];
+  }
+  cudaMemcpy(s->fmu, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice);
+  cudaMemcpy(s->tmu, t.data(), t.size() * sizeof(float), cudaMemcpyHostToDevice);
+}
+
+// One training step on `rows` raw feature rows X (device, [rows][kFeat]) and
+// standardised targets T (device, [rows][N]).  Returns the mean loss (after
+// the step's forward pass) when `sync`.
+float surrogate_train_step(Surrogate *s, const float *X, const float *T, long long rows, float lr, float wd,
+                           cudaStream_t st, bool sync, cudaError_t *err) {
+  *err = ensure_acts(s, rows);
+  if (*err != cudaSuccess) return NAN;
+  standardize<<<blocks(rows * kFeat, 256), 256, 0, st>>>(X, s->fmu, s->fsd, s->xb, rows, kFeat);
+  cudaMemcpyAsync(s->tgt, T, rows * s->N * sizeof(float), cudaMemcpyDeviceToDevice, st);
+  forward(s, rows, st, true);
+  backward(s, rows, st);
+  s->steps += 1;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float bc1 = 1.f - std::pow(b1, (float)s->steps), bc2 = 1.f - std::pow(b2, (float)s->steps);
+  adamw<<<blocks(s->nparam, 256), 256, 0, st>>>(s->w, s->wb, s->grad, s->m1, s->m2, s->nparam, lr, b1, b2, 1e-8f, wd,
+                                                 bc1, bc2);
+  *err = cudaGetLastError();
+  if (!sync) return 0.f;
+  float l = 0.f;
+  cudaMemcpyAsync(&l, s->loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+  cudaStreamSynchronize(st);
+  return l;
+}
+
+// Loss and gradients (no update) for a batch: used to check the backward pass.
+cudaError_t surrogate_gradients(Surrogate *s, const float *X, const float *T, long long rows, float *grad_host,
+                                float *loss_host, cudaStream_t st) {
+  cudaError_t e = ensure_acts(s, rows);
+  if (e != cudaSuccess) return e;
+  standardize<<<blocks(rows * kFeat, 256), 256, 0, st>>>(X, s->fmu, s->fsd, s->xb, rows, kFeat);
+  cudaMemcpyAsync(s->tgt, T, rows * s->N * sizeof(float), cudaMemcpyDeviceToDevice, st);
+  forward(s, rows, st, true);
+  backward(s, rows, st);
+  cudaMemcpyAsync(grad_host, s->grad, s->nparam * sizeof(float), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(loss_host, s->loss, sizeof(float), cudaMemcpyDeviceToHost, st);
+  return cudaStreamSynchronize(st);
+}
+
+cudaError_t surrogate_get_params(Surrogate *s, float *host) {
+  return cudaMemcpy(host, s->w, s->nparam * sizeof(float), cudaMemcpyDeviceToHost);
+}
+
+cudaError_t surrogate_set_params(Surrogate *s, const float *host) {
+  cudaError_t e = cudaMemcpy(s->w, host, s->nparam * sizeof(float), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return e;
+  to_bf16<<<blocks(s->nparam, 256), 256>>>(s->w, s->wb, s->nparam);
+  return cudaDeviceSynchronize();
+}
+
+// Inference for a batch of cells: features -> MLP -> alternative guess
+// (device SoA, [N][ncells]), processed in chunks of `chunk` rows.
+constexpr long long kChunk = 1 << 18;  // inference rows per pass
+
+// Allocates what surrogate_predict needs for `ncells` cells (call outside
+// any stream capture).
+cudaError_t surrogate_prepare(Surrogate *s, long long ncells) {
+  cudaError_t e = ensure_acts(s, std::min(ncells, kChunk));
+  if (e != cudaSuccess) return e;
+  if (s->feat_cap < ncells) {
+    cudaFree(s->feat);
+    s->feat = nullptr;
+    e = cudaMalloc(&s->feat, ncells * kFeat * sizeof(float));
+    if (e != cudaSuccess) return e;
+    s->feat_cap = ncells;
+  }
+  if (s->guess_cap < ncells) {
+    cudaFree(s->guess);
+    s->guess = nullptr;
+    e = cudaMalloc(&s->guess, ncells * kOut * sizeof(double));
+    if (e != cudaSuccess) return e;
+    s->guess_cap = ncells;
+  }
+  return cudaSuccess;
+}
+
+double *surrogate_guess_buffer(Surrogate *s) { return s->guess; }
+
+// Inference for a batch of cells: features -> MLP -> alternative guess in the
+// surrogate's guess buffer (device SoA, [N][ncells]).  Launch-only (no
+// allocation, no synchronisation): capturable in a CUDA graph after
+// surrogate_prepare.
+cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st) {
+  const long long nc = a.ncells;
+  cudaError_t e = surrogate_features(n, a, s->feat, st);
+  if (e != cudaSuccess) return e;
+  for (long long r0 = 0; r0 < nc; r0 += kChunk) {
+    const long long rows = std::min(kChunk, nc - r0);
+    standardize<<<blocks(rows * kFeat, 256), 256, 0, st>>>(s->feat + r0 * kFeat, s->fmu, s->fsd, s->xb, rows, kFeat);
+    forward(s, rows, st, false);
+    outputs_to_guess<<<blocks(rows, 128), 128, 0, st>>>(s->y, kOut, s->tmu, s->tsd, n.N, rows, r0, nc, s->guess);
+  }
+  return cudaGetLastError();
+}
+
+// Standardised targets from converged molalities (device SoA [N][M]) into T [M][N].
+cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, float *T, cudaStream_t st) {
+  targets_from_molal<<<blocks(M, 128), 128, 0, st>>>(molal, M, s->N, s->tmu, s->tsd, T);
+  return cudaGetLastError();
+}
+
+int surrogate_nfeat() { return kFeat; }
+void surrogate_mark_trained(Surrogate *s, bool t) { s->trained = t; }
+bool surrogate_trained(const Surrogate *s) { return s->trained; }
+
+}  // namespace pfchem

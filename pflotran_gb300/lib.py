@@ -69,7 +69,107 @@ def load(build_if_missing=True):
     return l
 
 
-class ReactionStep:
+class SurrogateConfig(C.Structure):
+    _fields_ = [("epochs", C.c_int32), ("batch", C.c_int32), ("lr", C.c_float), ("weight_decay", C.c_float),
+                ("seed", C.c_uint64)]
+
+
+class SurrogateReport(C.Structure):
+    _fields_ = [("samples", C.c_int64), ("steps", C.c_int64), ("first_loss", C.c_float),
+                ("final_loss", C.c_float), ("train_ms", C.c_double)]
+
+
+def _surrogate_bind(l):
+    vp = C.c_void_p
+    l.pfchem_surrogate_features.argtypes = [vp, C.POINTER(abi.Cells), vp]
+    l.pfchem_surrogate_fit.argtypes = [vp, vp, vp, C.c_int64, C.POINTER(SurrogateConfig),
+                                       C.POINTER(SurrogateReport)]
+    l.pfchem_surrogate_enable.argtypes = [vp, C.c_int]
+    l.pfchem_surrogate_predict.argtypes = [vp, C.POINTER(abi.Cells), vp]
+    l.pfchem_surrogate_gradients.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
+    l.pfchem_surrogate_gradients.restype = C.c_int64
+    l.pfchem_surrogate_params.argtypes = [vp, vp, C.c_int]
+    l.pfchem_surrogate_params.restype = C.c_int64
+    l.pfchem_surrogate_normalization.argtypes = [vp, vp, vp, vp, vp, C.c_int]
+
+
+class WarmStartMixin:
+    """Learned warm start on a ReactionStep (all tensors on the device)."""
+
+    def surrogate_features(self, cells):
+        import torch
+        _surrogate_bind(self._lib)
+        X = torch.empty((cells.ncells, 16), dtype=torch.float32, device="cuda")
+        s = cells.struct()
+        self._check(self._lib.pfchem_surrogate_features(self._ctx, C.byref(s), C.c_void_p(X.data_ptr())),
+                    "pfchem_surrogate_features")
+        return X
+
+    def surrogate_fit(self, X, molal_soa, epochs=8, batch=8192, lr=2e-3, weight_decay=1e-4, seed=7):
+        _surrogate_bind(self._lib)
+        M = X.shape[0]
+        cfg = SurrogateConfig(epochs, batch, lr, weight_decay, seed)
+        rep = SurrogateReport()
+        self._check(self._lib.pfchem_surrogate_fit(self._ctx, C.c_void_p(X.data_ptr()),
+                                                   C.c_void_p(molal_soa.data_ptr()), M, C.byref(cfg),
+                                                   C.byref(rep)), "pfchem_surrogate_fit")
+        return rep
+
+    def surrogate_predict(self, cells):
+        import torch
+        _surrogate_bind(self._lib)
+        g = torch.empty(self.network.N * cells.ncells, dtype=torch.float64, device="cuda")
+        s = cells.struct()
+        self._check(self._lib.pfchem_surrogate_predict(self._ctx, C.byref(s), C.c_void_p(g.data_ptr())),
+                    "pfchem_surrogate_predict")
+        return g
+
+    def surrogate_enable(self, on=True):
+        _surrogate_bind(self._lib)
+        self._check(self._lib.pfchem_surrogate_enable(self._ctx, int(on)), "pfchem_surrogate_enable")
+
+    def surrogate_gradients(self, X, molal_soa):
+        import numpy as np
+        _surrogate_bind(self._lib)
+        n = self._lib.pfchem_surrogate_params(self._ctx, None, 0)
+        g = np.zeros(n, np.float32)
+        loss = np.zeros(1, np.float32)
+        r = self._lib.pfchem_surrogate_gradients(self._ctx, C.c_void_p(X.data_ptr()),
+                                                 C.c_void_p(molal_soa.data_ptr()), X.shape[0],
+                                                 g.ctypes.data, loss.ctypes.data)
+        self._check(r, "pfchem_surrogate_gradients")
+        return g, float(loss[0])
+
+    def surrogate_params(self, values=None):
+        import numpy as np
+        _surrogate_bind(self._lib)
+        n = self._lib.pfchem_surrogate_params(self._ctx, None, 0)
+        self._check(n, "pfchem_surrogate_params")
+        if values is None:
+            out = np.zeros(n, np.float32)
+            self._lib.pfchem_surrogate_params(self._ctx, out.ctypes.data, 0)
+            return out
+        v = np.ascontiguousarray(values, np.float32)
+        assert v.size == n
+        self._check(self._lib.pfchem_surrogate_params(self._ctx, v.ctypes.data, 1), "pfchem_surrogate_params")
+
+    def surrogate_normalization(self, values=None):
+        import numpy as np
+        _surrogate_bind(self._lib)
+        N = self.network.N
+        if values is None:
+            fm, fs, tm, ts = (np.zeros(16, np.float32), np.zeros(16, np.float32), np.zeros(N, np.float32),
+                              np.zeros(N, np.float32))
+            self._check(self._lib.pfchem_surrogate_normalization(self._ctx, fm.ctypes.data, fs.ctypes.data,
+                                                                 tm.ctypes.data, ts.ctypes.data, 0), "norm")
+            return fm, fs, tm, ts
+        fm, fs, tm, ts = [np.ascontiguousarray(a, np.float32) for a in values]
+        self._check(self._lib.pfchem_surrogate_normalization(self._ctx, fm.ctypes.data, fs.ctypes.data,
+                                                             tm.ctypes.data, ts.ctypes.data, 1), "norm")
+
+
+
+class ReactionStep(WarmStartMixin):
     """Batched operator-split reaction step on one GPU."""
 
     def __init__(self, network, options=None, device=0):
