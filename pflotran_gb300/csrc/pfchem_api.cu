@@ -24,12 +24,13 @@ cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int g
                          cudaStream_t st);
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
-int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err);
+int gen_kernel(const DevNet &n, int block, void **fn_out, void **pro_out, std::string *err);
+int gen_prep_fields(const DevNet &n);
 int gen_blocks_per_sm(void *fn, const DevNet &n, int block);
 size_t gen_shared_bytes(const DevNet &n, int block);
 std::string generate_source(const DevNet &n, int block);
-cudaError_t gen_launch(void *fn, const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
-                       cudaStream_t st);
+cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, Scratch *scr, double *prep, int grid,
+                       int block, int refill, cudaStream_t st);
 struct Surrogate;
 Surrogate *surrogate_create(int N, uint64_t seed, std::string *err);
 void surrogate_destroy(Surrogate *s);
@@ -75,7 +76,10 @@ struct pfchem_ctx {
   CellArgs graph_args{};
   pfchem_launch graph_launch{};
   void *gen_fn = nullptr;  // specialized kernel for gen_block threads per block
+  void *gen_pro = nullptr; // its data-parallel prologue
   int gen_block = 0;
+  double *prep = nullptr;  // prologue records, gen_prep_fields x prep_cells doubles
+  int64_t prep_cells = 0;
   Surrogate *sur = nullptr;  // learned warm start
   bool sur_on = false;
   float norm[2 * 16 + 2 * PFCHEM_MAX_PRI] = {};  // host copy of the standardisation
@@ -274,12 +278,13 @@ void default_launch(pfchem_ctx *c) {
 int ensure_gen(pfchem_ctx *c, int block) {
   if (c->gen_fn && c->gen_block == block) return gen_blocks_per_sm(c->gen_fn, c->net, block);
   std::string e;
-  void *fn = nullptr;
-  if (gen_kernel(c->net, block, &fn, &e) != 0) {
+  void *fn = nullptr, *pro = nullptr;
+  if (gen_kernel(c->net, block, &fn, &pro, &e) != 0) {
     fail(c, -2, "specialized kernel: %s", e.c_str());
     return 0;
   }
   c->gen_fn = fn;
+  c->gen_pro = pro;
   c->gen_block = block;
   int nb = gen_blocks_per_sm(fn, c->net, block);
   if (nb < 1) fail(c, -1, "specialized kernel with %d threads per block does not fit on an SM", block);
@@ -366,6 +371,17 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
   }
   const pfchem_launch &L = c->launch;
   const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
+  if (L.variant == PFCHEM_KERNEL_SPECIALIZED && c->prep_cells < a.ncells) {
+    if (c->prep) cudaFree(c->prep);
+    c->prep = nullptr;
+    c->prep_cells = 0;
+    if (c->graph) {
+      cudaGraphExecDestroy(c->graph);
+      c->graph = nullptr;
+    }
+    CUDA_TRY(c, cudaMalloc(&c->prep, (size_t)gen_prep_fields(n) * a.ncells * sizeof(double)));
+    c->prep_cells = a.ncells;
+  }
   const bool same = c->graph && std::memcmp(&a, &c->graph_args, sizeof(CellArgs)) == 0 &&
                     std::memcmp(&L, &c->graph_launch, sizeof(pfchem_launch)) == 0;
   if (!same) {
@@ -379,7 +395,8 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
     cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream);
     cudaError_t pe = predict ? surrogate_predict(c->sur, n, a, c->stream) : cudaSuccess;
     cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
-                         ? gen_launch(c->gen_fn, n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream)
+                         ? gen_launch(c->gen_fn, c->gen_pro, n, a, c->scratch, c->prep, grid, L.block_threads,
+                                      L.refill_min_idle, c->stream)
                          : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
     if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
@@ -518,6 +535,7 @@ void pfchem_destroy(pfchem_ctx *c) {
   cudaSetDevice(c->device);
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->sur) surrogate_destroy(c->sur);
+  if (c->prep) cudaFree(c->prep);
   for (auto &b : c->stage)
     if (b.ptr) cudaFree(b.ptr);
   if (c->scratch) cudaFree(c->scratch);

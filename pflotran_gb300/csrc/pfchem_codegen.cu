@@ -549,7 +549,6 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     o << "  int st = evaluate_jac(L, Jb); if (st) return st;\n";
     o << "  bool bad; const bool conv = converged(L, &bad);\n";
     o << "  if (bad) return " << PFCHEM_CELL_NONFINITE << ";\n";
-    o << "  if (L.alt_pending) { L.alt_pending = false; if (rnorm(L) > L.rplain) return -2; L.alt_used = true; }\n";
     o << "  if (conv) return " << PFCHEM_CELL_CONVERGED << ";\n";
     o << "  if (L.iter >= " << n.max_iter << ") return " << PFCHEM_CELL_MAXITER << ";\n";
     if (!n.use_log) {
@@ -632,19 +631,95 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     o << "  if (a.iters) a.iters[cell] = L.iter;\n  if (a.status) a.status[cell] = status;\n}\n";
   }
 
-  void alt_guess() {
-    o << "__device__ __forceinline__ void arm_alt_guess(Lane &L, const CellArgs &a, long long cell, double *Jb) {\n";
-    o << "  evaluate_res(L, Jb); bool bad; converged(L, &bad);\n";
-    o << "  L.rplain = bad ? 1.7976931348623157e308 : rnorm(L);\n  const long long nc = a.ncells;\n";
+  // Per-cell record the prologue writes for the solve kernel (SoA, stride
+  // ncells): free-ion molalities and their logs at the chosen starting
+  // guess, ln gamma and gamma of the primaries, the fixed accumulation, the
+  // complex/mineral/surface constants, the ion-exchange warm starts, and
+  // whether the alternative guess was taken.
+  int prep_fields() const {
+    return 5 * n.N + n.Nc + (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? n.Nc : 0) + 2 * n.Nm + n.Nsc +
+           n.Nix + 1;
+  }
+  void prep_io(bool store) {
+    int f = 0;
+    auto fld = [&](const std::string &lane) {
+      if (store) o << "  prep[" << f << " * nc + cell] = " << lane << ";\n";
+      else o << "  " << lane << " = prep[" << f << " * nc + cell];\n";
+      ++f;
+    };
+    for (int j = 0; j < n.N; ++j) fld("L.m[" + I(j) + "]");
+    for (int j = 0; j < n.N; ++j) fld("L.lm[" + I(j) + "]");
+    for (int j = 0; j < n.N; ++j) fld("L.lg[" + I(j) + "]");
+    for (int j = 0; j < n.N; ++j) fld("L.g[" + I(j) + "]");
+    for (int j = 0; j < n.N; ++j) fld("L.fx[" + I(j) + "]");
+    for (int i = 0; i < n.Nc; ++i) fld("L.bc[" + I(i) + "]");
+    if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER)
+      for (int i = 0; i < n.Nc; ++i) fld("L.bK[" + I(i) + "]");
+    for (int k = 0; k < n.Nm; ++k) fld("L.bm[" + I(k) + "]");
+    for (int k = 0; k < n.Nm; ++k) fld("L.rk[" + I(k) + "]");
+    for (int k = 0; k < n.Nsc; ++k) fld("L.bs[" + I(k) + "]");
+    for (int r = 0; r < n.Nix; ++r) fld("L.ixr[" + I(r) + "]");
+    if (store) o << "  prep[" << f << " * nc + cell] = L.alt_used ? 1.0 : 0.0;\n";
+    else o << "  L.alt_used = prep[" << f << " * nc + cell] != 0.0;\n";
+  }
+
+  // Data-parallel prologue: one thread per cell, every lane busy.  It does
+  // all per-cell work that does not iterate -- log K, activity terms, fixed
+  // accumulation, logs of the guess -- and, given an alternative guess,
+  // evaluates the residual at both guesses and keeps the better one.
+  void prologue() {
+    o << "extern \"C\" __global__ void __launch_bounds__(128) pfchem_gen_prologue(const __grid_constant__ CellArgs a, "
+         "double *prep, double inv_dt, Scratch *scr) {\n";
+    o << "  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;\n";
+    o << "  const long long nc = a.ncells;\n  bool used = false;\n";
+    o << "  if (cell < nc && !(a.active && a.active[cell] <= 0)) {\n";
+    o << "  Lane L;\n  setup(L, a, cell, inv_dt);\n";
+    o << "  if (a.alt_guess) {\n";
+    o << "    evaluate_res(L, nullptr); bool bad; converged(L, &bad);\n";
+    o << "    const double rplain = bad ? 1.7976931348623157e308 : rnorm(L);\n";
+    o << "    double pm[NP], plm[NP], pix[NIX];\n";
+    o << "    for (int j = 0; j < NP; ++j) { pm[j] = L.m[j]; plm[j] = L.lm[j]; }\n";
+    o << "    for (int r = 0; r < NIX; ++r) pix[r] = L.ixr[r];\n";
+    o << "    bool ok = true;\n";
     for (int j = 0; j < n.N; ++j)
-      o << "  { const double g = a.alt_guess[" << j << " * nc + cell]; if (g > 0.0 && g <= 1.7976931348623157e308) { L.m["
-        << j << "] = g; L.lm[" << j << "] = log(g); } }\n";
-    o << "  L.alt_pending = true;\n}\n";
+      o << "    { const double g = a.alt_guess[" << j << " * nc + cell]; if (g > 0.0 && g <= 1.7976931348623157e308) { L.m["
+        << j << "] = g; L.lm[" << j << "] = xlog(g); } else ok = false; }\n";
+    o << "    double ralt = 1.7976931348623157e308;\n";
+    o << "    if (ok) { const int st = evaluate_res(L, nullptr); converged(L, &bad); if (!bad && st == 0) ralt = rnorm(L); }\n";
+    o << "    if (ralt <= rplain) { L.alt_used = true; used = true; }\n";
+    o << "    else { for (int j = 0; j < NP; ++j) { L.m[j] = pm[j]; L.lm[j] = plm[j]; } for (int r = 0; r < NIX; ++r) L.ixr[r] = pix[r]; }\n";
+    o << "  }\n";
+    prep_io(true);
+    o << "  }\n";
+    o << "  const unsigned bal = __ballot_sync(0xffffffffu, used);\n";
+    o << "  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&scr->alt_used, (unsigned long long)__popc(bal));\n";
+    o << "}\n";
+  }
+
+  // The solve kernel's per-cell start: the prologue's record plus the
+  // per-cell scalars that cost no FP64 work worth moving.
+  void load_prep() {
+    o << "__device__ __forceinline__ void load_prep(Lane &L, const CellArgs &a, long long cell, const double *prep, "
+         "double inv_dt) {\n";
+    o << "  const long long nc = a.ncells;\n";
+    o << "  const double por = a.por[cell], sat = a.sat[cell], vol = a.vol[cell], den = a.den[cell];\n";
+    o << "  L.por = por; L.vol = vol; L.dtc = a.dt;\n";
+    if (need_rho()) o << "  L.rho_s = a.rho_s[cell];\n";
+    o << "  L.acc = " << (n.accum_mode == PFCHEM_ACCUM_DT_CONSISTENT ? "inv_dt" : "1.0") << ";\n";
+    o << "  const double psv = por * sat * 1000.0 * vol;\n";
+    o << "  L.den_L = den * 1e-3; L.psv_den = psv * L.den_L; L.jac_aq = psv * inv_dt * L.den_L; L.v_t = vol * inv_dt;\n";
+    for (int k = 0; k < n.Nm; ++k)
+      o << "  L.vf[" << k << "] = a.vf[" << k << " * nc + cell]; L.ar[" << k << "] = a.area[" << k
+        << " * nc + cell]; L.rate[" << k << "] = 0.0;\n";
+    for (int r = 0; r < n.Nsr; ++r) o << "  L.srf[" << r << "] = a.srfree[" << r << " * nc + cell];\n";
+    prep_io(false);
+    o << "  L.Icell = a.ionic[cell]; L.Iacc = 0.0; L.Csum = 0.0;\n";
+    o << "  L.iter = 0; L.alt_pending = false;\n}\n";
   }
 
   void kernel() {
     o << "extern \"C\" __global__ void __launch_bounds__(" << js << ") pfchem_gen_react(const __grid_constant__ CellArgs a, "
-         "Scratch *scr, int refill_min_idle, double inv_dt) {\n";
+         "Scratch *scr, int refill_min_idle, double inv_dt, const double *prep) {\n";
     o << "  extern __shared__ double smem[];\n  double *Jb = smem + threadIdx.x;\n";
     o << "  long long *Eb = (long long *)(smem + " << n.N * (n.N + 1) * js << ") + threadIdx.x;\n";
     o << R"(  const unsigned full = 0xffffffffu;
@@ -673,8 +748,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
             if (a.iters) a.iters[cell] = 0;
             cell = -1;
           } else {
-            setup(L, a, cell, inv_dt);
-            if (a.alt_guess) arm_alt_guess(L, a, cell, Jb);
+            load_prep(L, a, cell, prep, inv_dt);
           }
         } else {
           exhausted = true;
@@ -688,15 +762,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     }
     if (cell >= 0) {
       int st = newton_step(L, Jb, Eb);
-      if (st == -2) {
-        const long long nc = a.ncells;
-        for (int j = 0; j < NP; ++j) { L.m[j] = a.pri_molal[j * nc + cell]; L.lm[j] = log(L.m[j]); }
-        L.iter = 0;
-        for (int r = 0; r < NIX; ++r) if (r < )" << n.Nix << R"() L.ixr[r] = a.ixref[r * nc + cell];
-        st = -1;
-      }
       if (st >= 0) {
-        my_alt += L.alt_used ? 1 : 0;
         finalize(L, a, cell, st);
         my_iters += L.iter;
         my_max = max(my_max, (unsigned)L.iter);
@@ -713,7 +779,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   }
   if (lane == 0) {
     atomicAdd(&scr->sum_iter, my_iters);
-    atomicAdd(&scr->alt_used, my_alt);
+    (void)my_alt;
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);
   }
@@ -730,7 +796,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     solve();
     newton_step();
     finalize();
-    alt_guess();
+    prologue();
+    load_prep();
     kernel();
     return o.str();
   }
@@ -738,7 +805,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
 
 struct Loaded {
   CUmodule mod = nullptr;
-  CUfunction fn = nullptr;
+  CUfunction fn = nullptr;   // persistent solve kernel
+  CUfunction pro = nullptr;  // data-parallel prologue
 };
 
 // Driver-API entry points, resolved through the runtime so that the library
@@ -789,7 +857,7 @@ size_t gen_shared_bytes(const DevNet &n, int block) {
 
 // Compiles (or fetches from the per-process cache) the specialized kernel for
 // `n` and `block` threads per block on the current device.
-int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err) {
+int gen_kernel(const DevNet &n, int block, void **fn_out, void **pro_out, std::string *err) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaFree(0);  // make the device's primary context current for the driver API
@@ -799,6 +867,7 @@ int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err) {
   auto it = g_cache.find(key);
   if (it != g_cache.end()) {
     *fn_out = (void *)it->second.fn;
+    *pro_out = (void *)it->second.pro;
     return 0;
   }
   nvrtcProgram prog;
@@ -837,6 +906,7 @@ int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err) {
     return -2;
   }
   cr = D.moduleGetFunction(&L.fn, L.mod, "pfchem_gen_react");
+  if (cr == CUDA_SUCCESS) cr = D.moduleGetFunction(&L.pro, L.mod, "pfchem_gen_prologue");
   if (cr != CUDA_SUCCESS) {
     *err = "cuModuleGetFunction failed";
     return -2;
@@ -844,7 +914,13 @@ int gen_kernel(const DevNet &n, int block, void **fn_out, std::string *err) {
   D.funcSetAttribute(L.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024);
   g_cache[key] = L;
   *fn_out = (void *)L.fn;
+  *pro_out = (void *)L.pro;
   return 0;
+}
+
+int gen_prep_fields(const DevNet &n) {
+  Gen g(n, 32);
+  return g.prep_fields();
 }
 
 int gen_blocks_per_sm(void *fn, const DevNet &n, int block) {
@@ -854,15 +930,20 @@ int gen_blocks_per_sm(void *fn, const DevNet &n, int block) {
   return nb;
 }
 
-cudaError_t gen_launch(void *fn, const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
-                       cudaStream_t st) {
+// Prologue over all cells, then the persistent solve.
+cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, Scratch *scr, double *prep, int grid,
+                       int block, int refill, cudaStream_t st) {
   CellArgs args = a;
   double inv_dt = 1.0 / a.dt;
-  void *params[] = {&args, &scr, &refill, &inv_dt};
   const Driver &D = driver();
-  if (!D.ok || !fn) return cudaErrorLaunchFailure;
-  CUresult r = D.launchKernel((CUfunction)fn, grid, 1, 1, block, 1, 1, (unsigned)gen_shared_bytes(n, block),
-                              (CUstream)st, params, nullptr);
+  if (!D.ok || !fn || !pro) return cudaErrorLaunchFailure;
+  void *pparams[] = {&args, &prep, &inv_dt, &scr};
+  const unsigned pgrid = (unsigned)((a.ncells + 127) / 128);
+  CUresult r = D.launchKernel((CUfunction)pro, pgrid, 1, 1, 128, 1, 1, 0, (CUstream)st, pparams, nullptr);
+  if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;
+  void *params[] = {&args, &scr, &refill, &inv_dt, &prep};
+  r = D.launchKernel((CUfunction)fn, grid, 1, 1, block, 1, 1, (unsigned)gen_shared_bytes(n, block), (CUstream)st,
+                     params, nullptr);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
 }
 
