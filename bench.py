@@ -109,10 +109,12 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_workload(ncells, device="cpu"):
+def make_workload(ncells, device="cpu", rank=0):
+    """The synthetic 12-species workload; rank r of a multi-GPU run takes its
+    own seeded shard of cells (weak scaling, no data exchange)."""
     from pflotran_gb300 import workloads
     net = workloads.synthetic_network()
-    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024, net=net, device=device)
+    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024 + 7919 * rank, net=net, device=device)
     return net, opt, cells, dt
 
 
@@ -186,7 +188,7 @@ def main():
     from pflotran_gb300.cells import CellBatch
     from pflotran_gb300.lib import ReactionStep
 
-    net, opt, host, dt = make_workload(args.ncells, device=f"cuda:{local}")
+    net, opt, host, dt = make_workload(args.ncells, device=f"cuda:{local}", rank=rank)
     n = host.ncells
     step = ReactionStep(net, opt, device=local)
     pristine = host.to_device()
