@@ -37,6 +37,9 @@ sys.path.insert(0, ROOT)
 METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start vs plain GPU Newton"
 UNIT = "cell solves/s"
 NCELLS = 2_097_152
+# DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
+# on 131,072 cells of the same workload (154.0 MB read + 51.1 MB written)
+TRAFFIC_BYTES_PER_CELL = (154023168 + 51135488) / 131072
 
 
 def parse():
@@ -52,6 +55,8 @@ def parse():
     p.add_argument("--train-samples", type=int, default=8_388_608)
     p.add_argument("--epochs", type=int, default=12)
     p.add_argument("--plain-only", action="store_true")
+    p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
+                   help="also time the step with the exact Newton Jacobian")
     return p.parse_args()
 
 
@@ -208,7 +213,7 @@ def main():
             restore()
             step.react(dev, dt)
         torch.cuda.synchronize()
-        dev_ms, iters, alt = [], [], []
+        dev_ms, iters, alt, slots = [], [], [], []
         with Clocks(clk_index) as clk:
             for _ in range(args.steps):
                 restore()
@@ -220,11 +225,13 @@ def main():
                 dev_ms.append(st.kernel_ms)
                 iters.append(st.sum_iterations)
                 alt.append(st.alt_guess_used)
+                slots.append(st.lane_slots)
                 torch.cuda.synchronize()
-        return float(np.sum(dev_ms)), iters, alt, clk.summary()
+        eff = float(np.sum(iters)) / float(np.sum(slots)) if np.sum(slots) else None
+        return float(np.sum(dev_ms)), iters, alt, clk.summary(), eff
 
     # plain Newton from the previous-step guess
-    plain_ms, plain_iters, _, plain_clocks = timed(local)
+    plain_ms, plain_iters, _, plain_clocks, plain_eff = timed(local)
     plain_value = world * n / (plain_ms / args.steps * 1e-3)
     g_plain = dev.to_host()
     warm = None
@@ -253,15 +260,47 @@ def main():
         warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),
                     err0_rms=float(err0.pow(2).mean().sqrt()), err0_p50=float(err0.max(0).values.median()))
-    total_ms, iters, alt, clocks = timed(local) if warm is not None else (plain_ms, plain_iters, [0], plain_clocks)
+    total_ms, iters, alt, clocks, eff = (timed(local) if warm is not None
+                                         else (plain_ms, plain_iters, [0], plain_clocks, plain_eff))
     launch = step.launch()
+    g = dev.to_host()
+    exact = None
+    if args.exact_jacobian:
+        # the same step with the exact Newton Jacobian (same equations and root)
+        from pflotran_gb300 import abi
+        from pflotran_gb300.network import default_options
+        step.set_options(default_options(use_isothermal=opt.use_isothermal, jacobian=abi.JACOBIAN_EXACT))
+        exact = {}
+        for mode in (("plain", "warm") if warm is not None else ("plain",)):
+            if warm is not None:
+                step.surrogate_enable(mode == "warm")
+            if args.autotune:
+                restore()
+                step.autotune(dev, dt)
+            ms, its, _, _, e_eff = timed(local)
+            ge = dev.to_host()
+            both = (ge.status == 0) & (g.status == 0)
+            rel = np.abs(ge.total_out - g.total_out).reshape(net.N, n) / np.maximum(
+                np.abs(g.total_out).reshape(net.N, n), 1e-300)
+            exact[mode] = {"value": world * n / (ms / args.steps * 1e-3), "ms_per_step": ms / args.steps,
+                           "mean_newton_iterations": float(np.mean(its)) / n,
+                           "max_newton_iterations": int(ge.iterations.max()),
+                           "lane_efficiency": e_eff,
+                           "nonconverged": int((ge.status != 0).sum()),
+                           "total_rel_diff_vs_reference_jacobian_max": float(rel[:, both].max())}
+        if warm is not None:
+            exact["speedup_warm_vs_plain"] = exact["warm"]["value"] / exact["plain"]["value"]
+            exact["speedup_vs_reference_jacobian_warm"] = exact["warm"]["value"] / (world * n / (total_ms / args.steps * 1e-3))
+        step.set_options(opt)
+        step.set_launch(launch.block_threads, launch.blocks_per_sm, launch.refill_min_idle, launch.variant)
+        if warm is not None:
+            step.surrogate_enable(True)
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
     value = world * n / (ms_per_step * 1e-3)
-    g = dev.to_host()
     conv = int((g.status == 0).sum())
 
     # end-to-end through the public API with pinned host buffers
@@ -315,6 +354,7 @@ def main():
         r = warm["report"]
         wline = {"plain_value": plain_value, "plain_ms_per_step": plain_ms / args.steps,
                  "plain_mean_newton_iterations": float(np.mean(plain_iters)) / n,
+                 "plain_lane_efficiency": plain_eff,
                  "speedup_vs_plain": value / plain_value,
                  "alt_guess_used_frac": float(np.mean(alt)) / n,
                  "surrogate": {"arch": "16-256-256-256-12 GELU MLP, BF16 weights/activations, FP32 accumulate "
@@ -337,10 +377,15 @@ def main():
                               "refill_min_idle": launch.refill_min_idle},
                    "parallelism": "replicas" if world > 1 else "single"},
         "mean_newton_iterations": mean_iters, "converged_cells": conv,
+        "lane_efficiency": eff,
         "iteration_histogram": np.bincount(g.iterations).tolist(),
         "gpu_launches": args.steps * (1 if warm is None else 2 + 6 * ((n + 262143) // 262144)),
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": probe, "unit": "TFLOP/s",
-                     "frac": achieved_tflops / probe if probe else None, "traffic": None,
+                     "frac": achieved_tflops / probe if probe else None,
+                     "traffic": TRAFFIC_BYTES_PER_CELL * n,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pfchem_gen_react "
+                                       "launch on 131072 cells, scaled by cells "
+                                       "(profiles/pfchem_gen_react_synthetic12_131k.md)",
                      "peak_source": "measured DFMA throughput on this GPU (pfchem_probe_fp64_peak, FMA = 2 flops)",
                      "flops_per_step": flops,
                      "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
@@ -348,6 +393,8 @@ def main():
         "clocks": clocks,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
+    if exact is not None:
+        line["exact_jacobian"] = exact
     if wline is not None:
         line["warm_start"] = wline
         line["config"]["workload"] = line["config"]["workload"].replace(

@@ -166,8 +166,23 @@ typedef struct pfchem_options {
   double max_relative_change_tolerance; /* reaction%max_relative_change_tolerance (1e-6); <= 0 disables */
   double max_residual_tolerance;      /* reaction%max_residual_tolerance (1e-12) */
   int32_t update_kinetic_state;       /* 1: fuse RUpdateKineticState after the solve */
-  int32_t reserved1;
+  int32_t jacobian;                   /* PFCHEM_JACOBIAN_* (0 = the reference's) */
 } pfchem_options;
+/* Newton Jacobian.  REFERENCE forms it as RReact does, with three
+ * inexact terms that make Newton converge linearly:
+ *  - RTotalSorbEqSurfCplx1 adds the free-site part of dS_k/dm_j only for the
+ *    components j of complex k (reaction_surf_complex.F90:905-931), although
+ *    the free-site concentration depends on every component on the site;
+ *  - RKineticMineral divides by |affinity| where the derivative has the
+ *    signed affinity (reaction_mineral.F90:842-846), so the mineral term has
+ *    the wrong sign for a precipitating mineral, and
+ *  - it scales dQK/dm by den_kg/1000 (reaction_mineral.F90:867,885), and
+ *    keeps dQK/dm where QK is capped at 1e3 (reaction_mineral.F90:699-703).
+ * EXACT (no counterpart in the reference) uses the derivatives of the same
+ * residual: same equations, same root, fewer iterations; the rate-limiter
+ * branch keeps the reference's expression apart from the affinity sign. */
+#define PFCHEM_JACOBIAN_REFERENCE 0
+#define PFCHEM_JACOBIAN_EXACT 1
 
 /* One batch of cells.  Pointers are all device pointers (on_device = 1) or all
  * host pointers (on_device = 0; the library stages them through the device).
@@ -212,6 +227,9 @@ typedef struct pfchem_stats {
   int32_t nonconverged;    /* cells with status != CONVERGED/INACTIVE */
   int64_t alt_guess_used;  /* cells that started from alt_guess       */
   double kernel_ms;        /* device time of the solve kernel         */
+  int64_t lane_slots;      /* 32 x warp trips of Newton steps in the persistent
+                              kernel: sum_iterations / lane_slots is the share
+                              of SIMT lanes doing Newton work (0 if not counted) */
 } pfchem_stats;
 
 typedef struct pfchem_ctx pfchem_ctx;
@@ -250,6 +268,26 @@ int pfchem_react_batch_interleaved(pfchem_ctx *ctx, double dt, int32_t ncomp,
 /* Batched RUpdateKineticState (reaction.F90:5320-5429) at the current state,
  * replacing the cell loop of RTUpdateKineticState (reactive_transport.F90:692-705). */
 int pfchem_update_kinetic_state(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
+
+/* Stream-ordered variant for callers that keep the cells on the device and
+ * run their own transport update on the GPU (no counterpart in the reference,
+ * whose RTReact is synchronous and per cell).  pfchem_react_batch_async
+ * enqueues one reaction step -- statistics reset, warm-start inference when
+ * enabled, the prologue and the persistent solve -- on `stream` (a
+ * cudaStream_t) and returns without waiting.  It allocates nothing and
+ * synchronises nothing, so the caller may capture it into a CUDA graph
+ * together with its transport kernels and replay that graph step after step.
+ * Device pointers only.  The context's buffers must first be reserved for at
+ * least cells->ncells cells with pfchem_reserve (outside any capture);
+ * otherwise the call fails and enqueues nothing.  One step may be in flight
+ * per context: the statistics counters are per context.
+ * pfchem_async_stats reads those counters once the caller has synchronised
+ * `stream` after the step (kernel_ms is 0: time the step on the caller's
+ * stream).  pfchem_reserve also sizes the warm-start buffers when a surrogate
+ * exists (fit it before reserving). */
+int pfchem_reserve(pfchem_ctx *ctx, int64_t ncells);
+int pfchem_react_batch_async(pfchem_ctx *ctx, double dt, pfchem_cells *cells, void *stream);
+int pfchem_async_stats(pfchem_ctx *ctx, pfchem_stats *stats);
 
 /* Statistics of the last react call: what the OS_STATISTICS block of RTReact
  * accumulates (reactive_transport.F90:1645-1804). */

@@ -37,6 +37,8 @@ def lib():
         l.pfo_interpolate_logK.argtypes = [C.c_void_p, C.c_double]
         l.pfo_interpolate_logK.restype = C.c_double
         l.pfo_ifc67_density.argtypes = [C.c_double, C.c_double]
+        l.pfo_newton_system.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_int64, C.c_void_p,
+                                        C.c_void_p, C.c_void_p]
         l.pfo_ifc67_density.restype = C.c_double
         _lib = l
     return _lib
@@ -95,3 +97,18 @@ def equilibrate_constraint(net_struct, opt, cells, types, conc):
     if r:
         raise RuntimeError(f"constraint equilibration failed ({r})")
     return int(it[0])
+
+
+def newton_system(net_struct, opt, dt, cells, k, m):
+    """RReact's residual F and Jacobian dF/dm (N x N) for cell k at molalities m."""
+    import numpy as np
+    N = len(m)
+    m = np.ascontiguousarray(m, np.float64)
+    F = np.zeros(N)
+    J = np.zeros(N * N)
+    s = cells.struct()
+    r = lib().pfo_newton_system(C.byref(net_struct), C.byref(opt), dt, C.byref(s), k, m.ctypes.data, F.ctypes.data,
+                                J.ctypes.data)
+    if r:
+        raise RuntimeError("pfo_newton_system failed")
+    return F, J.reshape(N, N)

@@ -28,6 +28,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -53,6 +54,7 @@ constexpr int NZ = PFCHEM_MAX_NNZ;
 struct Net {
   const pfchem_network *n;
   int N, Nc, Nm, Nix, Nsr, Nsc;
+  bool exact_jac = false;  // PFCHEM_JACOBIAN_EXACT
   int id(const int32_t *t, int ld, int k, int r) const { return t[(ld + 1) * r + k]; }
   double st(const double *t, int ld, int k, int r) const { return t[ld * (r) + (k - 1)]; }
   // aqueous complex icplx (0-based): count and 0-based species ids
@@ -383,6 +385,20 @@ int total_sorb_eq_surfcplx1(const Net &w, Cell<R> &c, int irxn) {
       c.total_sorb_eq[icomp] = c.total_sorb_eq[icomp] + R(w.snu(ic, i)) * srfcplx_conc[ic];
     }
     R nui_Si_over_Sx = R(n.srfcplx_free_site_stoich[ic]) * srfcplx_conc[ic] / free_site_conc;
+    if (w.exact_jac) {
+      // every component of the site moves the free-site concentration
+      R t[P];
+      for (int j = 0; j < N; ++j) t[j] = nui_Si_over_Sx * dSx_dmi[j];
+      for (int j = 1; j <= nc; ++j) {
+        int jcomp = w.sid(ic, j);
+        t[jcomp] = R(w.snu(ic, j)) * srfcplx_conc[ic] / c.pri_molal[jcomp] + t[jcomp];
+      }
+      for (int i = 1; i <= nc; ++i) {
+        int icomp = w.sid(ic, i);
+        for (int j = 0; j < N; ++j) c.dtotal_sorb_eq[icomp][j] = c.dtotal_sorb_eq[icomp][j] + R(w.snu(ic, i)) * t[j];
+      }
+      continue;
+    }
     for (int j = 1; j <= nc; ++j) {
       int jcomp = w.sid(ic, j);
       R t = R(w.snu(ic, j)) * srfcplx_conc[ic] / c.pri_molal[jcomp] + nui_Si_over_Sx * dSx_dmi[jcomp];
@@ -602,8 +618,9 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
     }
     if (!compute_derivative) continue;
     R dIm_dQK;
+    if (w.exact_jac && lnQK > R(6.90776)) continue;  // QK capped: the rate does not depend on m
     if (n.kinmnrl_affinity_power)
-      dIm_dQK = -Im * R(n.kinmnrl_affinity_power[m]) / std::fabs(affinity_factor);
+      dIm_dQK = -Im * R(n.kinmnrl_affinity_power[m]) / (w.exact_jac ? affinity_factor : std::fabs(affinity_factor));
     else
       dIm_dQK = -Im_const * sum_prefactor_rate;
     if (n.kinmnrl_Temkin_const) {
@@ -618,7 +635,7 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
       for (int j = 1; j <= ncomp; ++j) {
         int jc = w.mid(m, j);
         R dQK_dCj = R(w.mnu(m, j)) * QK * rexp(-ln_conc[jc]);
-        R dQK_dmj = dQK_dCj * c.den_kg * R(1e-3);
+        R dQK_dmj = w.exact_jac ? dQK_dCj : dQK_dCj * c.den_kg * R(1e-3);
         for (int i = 1; i <= ncomp; ++i) {
           int ic = w.mid(m, i);
           Jac[ic][jc] = Jac[ic][jc] + R(w.mnu(m, i)) * dIm_dQK * dQK_dmj;
@@ -630,7 +647,7 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
       for (int j = 1; j <= ncomp; ++j) {
         int jc = w.mid(m, j);
         R dQK_dCj = R(w.mnu(m, j)) * QK * rexp(-ln_conc[jc]);
-        R dQK_dmj = dQK_dCj * c.den_kg * R(1e-3);
+        R dQK_dmj = w.exact_jac ? dQK_dCj : dQK_dCj * c.den_kg * R(1e-3);
         for (int i = 1; i <= ncomp; ++i) {
           int ic = w.mid(m, i);
           Jac[ic][jc] = Jac[ic][jc] + R(w.mnu(m, i)) * dIm_dQK * (R(1) + QK / rl / den) * dQK_dmj / den;
@@ -811,11 +828,93 @@ void residual_scale(const Net &w, const pfchem_options &o, const Cell<R> &c, con
   (void)o;
 }
 
+// Residual of the step equations at the cell's current pri_molal, as the
+// Newton loop below forms it, and its norm in the units of the convergence
+// test (DBL_MAX when not finite).  Returns false when an inner sorption
+// iteration failed.  Used only for the choice between two starting guesses,
+// an addition of this library with no counterpart in RReact.
+template <class R>
+bool residual_norm(const Net &w, const pfchem_options &o, Cell<R> &c, const R *fixed_accum, R psv_t, R dt,
+                   R accum_scale, R *rnorm) {
+  const int N = w.N;
+  const bool sorb = (w.Nix + w.Nsr) > 0;
+  const bool inner_ok = auxvar_compute(w, c) == 0;
+  R residual[P], J[P][P];
+  for (int j = 0; j < N; ++j) {
+    if (o.accum_mode == PFCHEM_ACCUM_LITERAL) {
+      residual[j] = psv_t * c.total[j] - fixed_accum[j];
+      if (sorb) residual[j] = residual[j] + c.total_sorb_eq[j] * c.volume;
+    } else {
+      R acc = psv_t * c.total[j];
+      if (sorb) acc = acc + c.total_sorb_eq[j] * c.volume;
+      residual[j] = -fixed_accum[j] / dt + acc / dt;
+    }
+  }
+  if (w.Nm > 0) kinetic_mineral(w, c, residual, J, false);
+  bool nonfinite = false;
+  for (int j = 0; j < N; ++j)
+    if (!std::isfinite((double)residual[j])) nonfinite = true;
+  if (nonfinite) {
+    *rnorm = R(DBL_MAX);
+    return inner_ok;
+  }
+  R r = 0;
+  if (o.residual_tol_kind == PFCHEM_RESIDUAL_RELATIVE) {
+    R S[P];
+    residual_scale(w, o, c, fixed_accum, psv_t, accum_scale, S);
+    for (int j = 0; j < N; ++j) r = std::max(r, std::fabs(residual[j]) / S[j]);
+  } else {
+    for (int j = 0; j < N; ++j) r = std::max(r, std::fabs(residual[j]));
+  }
+  *rnorm = r;
+  return inner_ok;
+}
+
+// One Newton system of RReact at the cell's current pri_molal: auxiliary
+// variables, residual and Jacobian d residual / d m (reaction.F90:3415-3440).
+// Returns non-zero when an inner sorption iteration failed.
+template <class R>
+int newton_system(const Net &w, const pfchem_options &o, Cell<R> &c, const R *fixed_accum, R psv_t, R dt,
+                  R *residual, R (*J)[P]) {
+  const int N = w.N;
+  const bool sorb = (w.Nix + w.Nsr) > 0;
+  const R psvd_t = c.porosity * c.sat * R(1000) * c.volume / dt;
+  const R v_t = c.volume / dt;
+  if (auxvar_compute(w, c)) return 1;
+  // residual: the literal RReact order (reaction.F90:3424-3432), or the
+  // global-implicit order r = -accum/dt + (psv*T + V*S)/dt + R
+  // (reactive_transport.F90:2541-2564)
+  if (o.accum_mode == PFCHEM_ACCUM_LITERAL) {
+    for (int j = 0; j < N; ++j) residual[j] = psv_t * c.total[j] - fixed_accum[j];
+    if (sorb)
+      for (int j = 0; j < N; ++j) residual[j] = residual[j] + c.total_sorb_eq[j] * c.volume;
+  } else {
+    for (int j = 0; j < N; ++j) {
+      R acc = psv_t * c.total[j];
+      if (sorb) acc = acc + c.total_sorb_eq[j] * c.volume;
+      residual[j] = -fixed_accum[j] / dt + acc / dt;
+    }
+  }
+  // RTAccumulationDerivative (reaction.F90:5152-5232)
+  for (int i = 0; i < N; ++i)
+    for (int j = 0; j < N; ++j) J[i][j] = c.dtotal[i][j] * psvd_t;
+  if (sorb)  // RAccumulationSorbDerivative (reaction.F90:4575-4603)
+    for (int i = 0; i < N; ++i)
+      for (int j = 0; j < N; ++j) J[i][j] = J[i][j] + c.dtotal_sorb_eq[i][j] * v_t;
+  // RReaction -> RKineticMineral (reaction.F90:3515-3584)
+  if (w.Nm > 0) kinetic_mineral(w, c, residual, J, true);
+  return 0;
+}
+
 // ---------------------------------------------------------------------------
-// reaction.F90:3322-3511 RReact.  Returns the per-cell status.
+// reaction.F90:3322-3511 RReact.  Returns the per-cell status.  `alt`, when
+// given, is a second starting guess (the learned warm start): the residual
+// is evaluated at both guesses and Newton starts from `alt` when its norm is
+// no larger, keeping the ion-exchange warm start of the evaluation it chose
+// and the surface free-site state it was given.
 template <class R>
 int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, R dt, R I_start,
-           int *num_iterations_out) {
+           int *num_iterations_out, const double *alt = nullptr, bool *alt_used = nullptr) {
   const int N = w.N;
   const bool sorb = (w.Nix + w.Nsr) > 0;
   const R one_over_dt = R(1) / dt;
@@ -838,8 +937,27 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
     for (int j = 0; j < N; ++j) c.pri_act_coef[j] = 1;
     for (int i = 0; i < w.Nc; ++i) c.sec_act_coef[i] = 1;
   }
-  const R psvd_t = c.porosity * c.sat * R(1000) * c.volume / dt;
-  const R v_t = c.volume / dt;
+  if (alt) {
+    R srf[SR];
+    for (int r = 0; r < w.Nsr; ++r) srf[r] = c.srfcplxrxn_free_site_conc[r];
+    R rplain, ralt = R(DBL_MAX);
+    residual_norm(w, o, c, fixed_accum, psv_t, dt, accum_scale, &rplain);  // inner status not used here
+    const Cell<R> plain = c;
+    bool ok = true;
+    for (int j = 0; j < N; ++j) {
+      const double g = alt[j];
+      if (g > 0.0 && g <= DBL_MAX) c.pri_molal[j] = R(g);
+      else ok = false;
+    }
+    if (ok) {
+      R r;
+      if (residual_norm(w, o, c, fixed_accum, psv_t, dt, accum_scale, &r) && r < R(DBL_MAX)) ralt = r;
+    }
+    const bool take = ralt <= rplain;
+    if (!take) c = plain;
+    for (int r = 0; r < w.Nsr; ++r) c.srfcplxrxn_free_site_conc[r] = srf[r];
+    if (alt_used) *alt_used = take;
+  }
   int status = PFCHEM_CELL_CONVERGED;
   R residual[P], J[P][P], update[P], prev_solution[P], new_solution[P];
   for (;;) {
@@ -850,32 +968,10 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
         break;
       }
     }
-    if (auxvar_compute(w, c)) {
+    if (newton_system(w, o, c, fixed_accum, psv_t, dt, residual, J)) {
       status = PFCHEM_CELL_INNER_MAXITER;
       break;
     }
-    // residual: the literal RReact order (reaction.F90:3424-3432), or the
-    // global-implicit order r = -accum/dt + (psv*T + V*S)/dt + R
-    // (reactive_transport.F90:2541-2564)
-    if (o.accum_mode == PFCHEM_ACCUM_LITERAL) {
-      for (int j = 0; j < N; ++j) residual[j] = psv_t * c.total[j] - fixed_accum[j];
-      if (sorb)
-        for (int j = 0; j < N; ++j) residual[j] = residual[j] + c.total_sorb_eq[j] * c.volume;
-    } else {
-      for (int j = 0; j < N; ++j) {
-        R acc = psv_t * c.total[j];
-        if (sorb) acc = acc + c.total_sorb_eq[j] * c.volume;
-        residual[j] = -fixed_accum[j] / dt + acc / dt;
-      }
-    }
-    // RTAccumulationDerivative (reaction.F90:5152-5232)
-    for (int i = 0; i < N; ++i)
-      for (int j = 0; j < N; ++j) J[i][j] = c.dtotal[i][j] * psvd_t;
-    if (sorb)  // RAccumulationSorbDerivative (reaction.F90:4575-4603)
-      for (int i = 0; i < N; ++i)
-        for (int j = 0; j < N; ++j) J[i][j] = J[i][j] + c.dtotal_sorb_eq[i][j] * v_t;
-    // RReaction -> RKineticMineral (reaction.F90:3515-3584)
-    if (w.Nm > 0) kinetic_mineral(w, c, residual, J, true);
     bool nonfinite = false;
     R rmax = 0;
     for (int j = 0; j < N; ++j) {
@@ -1008,7 +1104,10 @@ void react_one(const Net &w, const pfchem_options &o, double dt, pfchem_cells *c
   R tran[P];
   for (int j = 0; j < w.N; ++j) tran[j] = cl->total[j * n + k];
   int iters = 0;
-  int status = rreact(w, o, c, tran, R(dt), R(cl->ionic_strength[k]), &iters);
+  double alt[P];
+  if (cl->alt_guess)
+    for (int j = 0; j < w.N; ++j) alt[j] = cl->alt_guess[j * n + k];
+  int status = rreact(w, o, c, tran, R(dt), R(cl->ionic_strength[k]), &iters, cl->alt_guess ? alt : nullptr);
   if (status == PFCHEM_CELL_CONVERGED && o.update_kinetic_state) update_kinetic_state(w, c, R(dt));
   for (int j = 0; j < w.N; ++j) {
     cl->pri_molal[j * n + k] = (double)c.pri_molal[j];
@@ -1039,8 +1138,9 @@ void react_one(const Net &w, const pfchem_options &o, double dt, pfchem_cells *c
   if (cl->status) cl->status[k] = status;
 }
 
-Net make_net(const pfchem_network *n) {
+Net make_net(const pfchem_network *n, const pfchem_options *o = nullptr) {
   Net w;
+  w.exact_jac = o && o->jacobian == PFCHEM_JACOBIAN_EXACT;
   w.n = n;
   w.N = n->naqcomp;
   w.Nc = n->neqcplx;
@@ -1060,7 +1160,7 @@ extern "C" {
 // double, 1 = long double.  Returns the number of non-converged cells.
 int pfo_react_batch(const pfchem_network *net, const pfchem_options *opt, double dt, pfchem_cells *cells,
                     int precision, int nthreads) {
-  Net w = make_net(net);
+  Net w = make_net(net, opt);
   if (w.N > P || w.Nc > C || w.Nm > M || w.Nix > IX || w.Nsr > SR || w.Nsc > SC) return -1;
   const int64_t n = cells->ncells;
   if (nthreads < 1) nthreads = 1;
@@ -1089,8 +1189,40 @@ int pfo_react_batch(const pfchem_network *net, const pfchem_options *opt, double
 // (freq != OFF) or unity.  Used by the input generators and the KATs.
 // Writes total (mol/L), sec_molal, total_sorb_eq, sorption warm starts and
 // the self-consistent ionic strength of the speciated state.
+// RReact's Newton system for cell k of `cells` at free-ion molalities m:
+// residual F (mol/s) and Jacobian J[i*N + j] = dF_i/dm_j as RReact forms
+// them, after the step's activity update at the cell's ionic strength.  Test
+// support for finite-difference checks of the Jacobian.
+int pfo_newton_system(const pfchem_network *net, const pfchem_options *opt, double dt, const pfchem_cells *cells,
+                      int64_t k, const double *m, double *F, double *Jout) {
+  Net w = make_net(net, opt);
+  const pfchem_options &o = *opt;
+  Cell<double> c;
+  load_cell(w, cells, k, c);
+  const int N = w.N;
+  const int64_t n = cells->ncells;
+  for (int j = 0; j < N; ++j) c.total[j] = cells->total[j * n + k];
+  update_temp_dependent_coefs(w, o, c);
+  const double psv_t = c.porosity * c.sat * 1000.0 * c.volume;
+  double fixed_accum[P];
+  for (int j = 0; j < N; ++j) fixed_accum[j] = psv_t * c.total[j];
+  if (w.Nix + w.Nsr > 0)
+    for (int j = 0; j < N; ++j) fixed_accum[j] += c.total_sorb_eq[j] * c.volume;
+  if (o.act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF) {
+    if (activity_coefficients(w, o, c, true, cells->ionic_strength[k])) return 1;
+  }
+  for (int j = 0; j < N; ++j) c.pri_molal[j] = m[j];
+  double res[P], J[P][P];
+  if (newton_system(w, o, c, fixed_accum, psv_t, dt, res, J)) return 1;
+  for (int i = 0; i < N; ++i) {
+    F[i] = res[i];
+    for (int j = 0; j < N; ++j) Jout[i * N + j] = J[i][j];
+  }
+  return 0;
+}
+
 int pfo_speciate(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells) {
-  Net w = make_net(net);
+  Net w = make_net(net, opt);
   const int64_t n = cells->ncells;
   for (int64_t k = 0; k < n; ++k) {
     Cell<double> c;
@@ -1339,7 +1471,7 @@ extern "C" {
 // strength (at the final state, recomputed as the next LAG update would).
 int pfo_equilibrate_constraint(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
                                const int *type, const double *conc, int *iters) {
-  Net w = make_net(net);
+  Net w = make_net(net, opt);
   Cell<double> c;
   load_cell(w, cells, 0, c);
   update_temp_dependent_coefs(w, *opt, c);

@@ -40,6 +40,8 @@ CELL_INACTIVE = 5
 
 KERNEL_SPECIALIZED = 0
 KERNEL_GENERIC = 1
+JACOBIAN_REFERENCE = 0
+JACOBIAN_EXACT = 1
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)
@@ -86,7 +88,7 @@ class Options(C.Structure):
         ("accum_mode", C.c_int32), ("max_iterations", C.c_int32),
         ("max_dlnC", C.c_double), ("max_relative_change_tolerance", C.c_double),
         ("max_residual_tolerance", C.c_double),
-        ("update_kinetic_state", C.c_int32), ("reserved1", C.c_int32),
+        ("update_kinetic_state", C.c_int32), ("jacobian", C.c_int32),
     ]
 
 
@@ -109,6 +111,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("ncells", C.c_int64), ("sum_iterations", C.c_int64), ("max_iterations", C.c_int32),
         ("nonconverged", C.c_int32), ("alt_guess_used", C.c_int64), ("kernel_ms", C.c_double),
+        ("lane_slots", C.c_int64),
     ]
 
 

@@ -49,6 +49,7 @@ cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, 
 cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, float *T, cudaStream_t st);
 void surrogate_mark_trained(Surrogate *s, bool t);
 bool surrogate_trained(const Surrogate *s);
+bool surrogate_ready(const Surrogate *s, long long ncells);
 }  // namespace pfchem
 
 using namespace pfchem;
@@ -82,6 +83,7 @@ struct pfchem_ctx {
   int64_t prep_cells = 0;
   Surrogate *sur = nullptr;  // learned warm start
   bool sur_on = false;
+  int64_t async_cells = 0;  // cells of the last pfchem_react_batch_async
   float norm[2 * 16 + 2 * PFCHEM_MAX_PRI] = {};  // host copy of the standardisation
   char err[2048] = {0};
 };
@@ -140,6 +142,9 @@ int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o
   n.accum_mode = o->accum_mode;
   n.max_iter = o->max_iterations;
   n.update_kin = o->update_kinetic_state != 0;
+  if (o->jacobian != PFCHEM_JACOBIAN_REFERENCE && o->jacobian != PFCHEM_JACOBIAN_EXACT)
+    return fail(c, -1, "unknown jacobian %d", o->jacobian);
+  n.jac_exact = o->jacobian == PFCHEM_JACOBIAN_EXACT;
   n.max_dlnC = o->max_dlnC;
   n.rel_change_tol = o->max_relative_change_tolerance;
   n.res_tol = o->max_residual_tolerance;
@@ -356,6 +361,41 @@ CellArgs device_args(const pfchem_cells *cl, double dt) {
   return a;
 }
 
+// Grows the prologue record buffer to `ncells` cells (drops the cached graph,
+// whose nodes point at the old buffer).
+int reserve_prep(pfchem_ctx *c, int64_t ncells) {
+  if (c->prep_cells >= ncells) return 0;
+  if (c->prep) cudaFree(c->prep);
+  c->prep = nullptr;
+  c->prep_cells = 0;
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
+  CUDA_TRY(c, cudaMalloc(&c->prep, (size_t)gen_prep_fields(c->net) * ncells * sizeof(double)));
+  c->prep_cells = ncells;
+  return 0;
+}
+
+// Enqueues one reaction step on `st`: statistics reset, warm-start inference
+// (when `predict`; a.alt_guess must then point at the surrogate's guess
+// buffer), the prologue and the persistent solve.  Allocates nothing.
+int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st) {
+  const DevNet &n = c->net;
+  const pfchem_launch &L = c->launch;
+  const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
+  cudaError_t me = cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), st);
+  if (me != cudaSuccess) return fail(c, -2, "statistics reset: %s", cudaGetErrorString(me));
+  cudaError_t pe = predict ? surrogate_predict(c->sur, n, a, st) : cudaSuccess;
+  if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
+  cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
+                       ? gen_launch(c->gen_fn, c->gen_pro, n, a, c->scratch, c->prep, grid, L.block_threads,
+                                    L.refill_min_idle, st)
+                       : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, st);
+  if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
+  return 0;
+}
+
 int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
   const DevNet &n = c->net;
   if (a_in.ncells == 0) {
@@ -370,17 +410,9 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
     a.alt_guess = surrogate_guess_buffer(c->sur);
   }
   const pfchem_launch &L = c->launch;
-  const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
-  if (L.variant == PFCHEM_KERNEL_SPECIALIZED && c->prep_cells < a.ncells) {
-    if (c->prep) cudaFree(c->prep);
-    c->prep = nullptr;
-    c->prep_cells = 0;
-    if (c->graph) {
-      cudaGraphExecDestroy(c->graph);
-      c->graph = nullptr;
-    }
-    CUDA_TRY(c, cudaMalloc(&c->prep, (size_t)gen_prep_fields(n) * a.ncells * sizeof(double)));
-    c->prep_cells = a.ncells;
+  if (L.variant == PFCHEM_KERNEL_SPECIALIZED) {
+    const int re = reserve_prep(c, a.ncells);
+    if (re) return re;
   }
   const bool same = c->graph && std::memcmp(&a, &c->graph_args, sizeof(CellArgs)) == 0 &&
                     std::memcmp(&L, &c->graph_launch, sizeof(pfchem_launch)) == 0;
@@ -392,15 +424,9 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
     }
     cudaGraph_t g;
     CUDA_TRY(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream);
-    cudaError_t pe = predict ? surrogate_predict(c->sur, n, a, c->stream) : cudaSuccess;
-    cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
-                         ? gen_launch(c->gen_fn, c->gen_pro, n, a, c->scratch, c->prep, grid, L.block_threads,
-                                      L.refill_min_idle, c->stream)
-                         : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, c->stream);
+    const int ee = enqueue_step(c, a, predict, c->stream);
     cudaError_t ce = cudaStreamEndCapture(c->stream, &g);
-    if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
-    if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
+    if (ee) return ee;
     if (ce != cudaSuccess) return fail(c, -2, "graph capture: %s", cudaGetErrorString(ce));
     cudaError_t ie = cudaGraphInstantiate(&c->graph, g, 0);
     cudaGraphDestroy(g);
@@ -422,6 +448,7 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
   c->stats.nonconverged = (int32_t)h.nonconverged;
   c->stats.alt_guess_used = (int64_t)h.alt_used;
   c->stats.kernel_ms = ms;
+  c->stats.lane_slots = 32 * (int64_t)h.newton_trips;
   return (int)h.nonconverged;
 }
 
@@ -611,6 +638,60 @@ int pfchem_update_kinetic_state(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   cudaError_t le = launch_kinetic_state(c->net, a, c->stream);
   if (le != cudaSuccess) return fail(c, -2, "kinetic-state launch: %s", cudaGetErrorString(le));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int pfchem_reserve(pfchem_ctx *c, int64_t ncells) {
+  if (!c) return -1;
+  if (!c->has_net) return fail(c, -1, "pfchem_set_network must be called first");
+  if (ncells < 0) return fail(c, -1, "ncells < 0");
+  cudaSetDevice(c->device);
+  int e = reserve_prep(c, ncells);
+  if (e) return e;
+  if (c->sur) {
+    cudaError_t pe = surrogate_prepare(c->sur, ncells);
+    if (pe != cudaSuccess) return fail(c, -2, "surrogate buffers: %s", cudaGetErrorString(pe));
+  }
+  return 0;
+}
+
+int pfchem_react_batch_async(pfchem_ctx *c, double dt, pfchem_cells *cl, void *stream) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device) return fail(c, -1, "pfchem_react_batch_async takes device pointers");
+  if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  if (!cl->total) return fail(c, -1, "total is null");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, dt);
+  c->async_cells = a.ncells;
+  if (a.ncells == 0) return 0;
+  if (c->launch.variant == PFCHEM_KERNEL_SPECIALIZED && c->prep_cells < a.ncells)
+    return fail(c, -1, "%lld cells exceed the reserved %lld: call pfchem_reserve first", (long long)a.ncells,
+                (long long)c->prep_cells);
+  const bool predict = c->sur && c->sur_on && surrogate_trained(c->sur) && !a.alt_guess;
+  if (predict) {
+    if (!surrogate_ready(c->sur, a.ncells))
+      return fail(c, -1, "warm-start buffers are not reserved for %lld cells: call pfchem_reserve first",
+                  (long long)a.ncells);
+    a.alt_guess = surrogate_guess_buffer(c->sur);
+  }
+  return enqueue_step(c, a, predict, (cudaStream_t)stream);
+}
+
+int pfchem_async_stats(pfchem_ctx *c, pfchem_stats *s) {
+  if (!c || !s) return -1;
+  cudaSetDevice(c->device);
+  Scratch h;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->scratch, sizeof(Scratch), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  *s = pfchem_stats{};
+  s->ncells = c->async_cells;
+  s->sum_iterations = (int64_t)h.sum_iter;
+  s->max_iterations = (int32_t)h.max_iter;
+  s->nonconverged = (int32_t)h.nonconverged;
+  s->alt_guess_used = (int64_t)h.alt_used;
+  s->kernel_ms = 0.0;
+  s->lane_slots = 32 * (int64_t)h.newton_trips;
   return 0;
 }
 

@@ -26,6 +26,7 @@
 #include <cuda_runtime.h>
 #include <nvrtc.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -33,6 +34,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <vector>
 #include <vector>
 
 #include "pfchem_device.cuh"
@@ -79,6 +81,47 @@ struct Gen {
     return n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? "L.bK[" + I(i) + "]" : "L.bc[" + I(i) + "]";
   }
   bool sorb() const { return n.Nix + n.Nsr > 0; }
+  // Mass-action products instead of exponentials: with activity
+  // coefficients fixed for the step, C_i = exp(bc_i + sum nu ln a) equals
+  // K_i * prod a^nu with K_i = exp(bc_i) computed once per cell, so the
+  // Newton iterations need multiplications where the log form needs one exp
+  // per complex.  Used when every stoichiometric coefficient is an integer
+  // in [-4, 4].
+  static bool small_int(double v) { return v == std::floor(v) && std::fabs(v) <= 4.0 && v != 0.0; }
+  bool prod_cplx() const {
+    if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) return false;
+    for (int i = 0; i < n.Nc; ++i)
+      for (int k = 0; k < n.cn[i]; ++k)
+        if (!small_int(n.cnu[i][k])) return false;
+    return true;
+  }
+  // surface complexes of closed-form sites (no free-site inner Newton)
+  bool prod_srf(int r) const {
+    if (n.srflag[r]) return false;
+    for (int q = 0; q < n.srn[r]; ++q) {
+      const int k = n.src[r][q];
+      for (int l = 0; l < n.sn[k]; ++l)
+        if (!small_int(n.snu[k][l])) return false;
+    }
+    return true;
+  }
+  bool prod_any() const {
+    if (prod_cplx() && n.Nc > 0) return true;
+    for (int r = 0; r < n.Nsr; ++r)
+      if (prod_srf(r)) return true;
+    return false;
+  }
+  // product of a^nu over the species of a reaction as a C expression
+  std::string prod_expr(const std::string &K, int cnt, const int8_t *ids, const double *nus) const {
+    std::string e = K;
+    for (int k = 0; k < cnt; ++k) {
+      const int j = ids[k];
+      const int v = (int)nus[k];
+      const std::string b = v > 0 ? "a" + I(j) : "ra" + I(j);
+      for (int t = 0; t < std::abs(v); ++t) e += " * " + b;
+    }
+    return e;
+  }
   bool act() const { return n.act_freq != PFCHEM_ACT_COEF_FREQUENCY_OFF; }
   bool any_h2o() const {
     for (int i = 0; i < n.Nc; ++i)
@@ -139,6 +182,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     bool needg[PFCHEM_MAX_PRI] = {};
     for (int r = 0; r < n.Nix; ++r)
       for (int k = 0; k < n.xn[r]; ++k) needg[n.xid[r][k]] = true;
+    if (prod_any())
+      for (int j = 0; j < n.N; ++j) needg[j] = true;
     for (int j = 0; j < n.N; ++j) {
       if (n.Z2p[j] > 1e-20) {
         o << "  L.lg[" << j << "] = (" << lit(-n.Z2p[j] * n.A) << " * sI / (1.0 + " << lit(n.ap[j] * n.B)
@@ -218,6 +263,13 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       for (int j = 0; j < n.N; ++j) o << "  L.lg[" << j << "] = 0.0; L.g[" << j << "] = 1.0;\n";
       for (int i = 0; i < n.Nc; ++i) o << "  L.bc[" << i << "] = " << bK(i) << ";\n";
     }
+    // product-form constants: exp of the log constants, once per cell
+    if (prod_cplx())
+      for (int i = 0; i < n.Nc; ++i) o << "  L.bc[" << i << "] = xexp(L.bc[" << i << "]);\n";
+    for (int r = 0; r < n.Nsr; ++r)
+      if (prod_srf(r))
+        for (int q = 0; q < n.srn[r]; ++q)
+          o << "  L.bs[" << (int)n.src[r][q] << "] = xexp(L.bs[" << (int)n.src[r][q] << "]);\n";
     o << "  L.Iacc = 0.0; L.Csum = 0.0;\n";
     o << "  L.iter = 0; L.alt_pending = false; L.alt_used = false;\n}\n";
   }
@@ -227,6 +279,24 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     const int N = n.N;
     o << "__device__ __forceinline__ int evaluate_" << (jac ? "jac" : "res") << "(Lane &L, double *Jb) {\n";
     o << "  int status = 0;\n";
+    if (prod_any()) {
+      bool neg[PFCHEM_MAX_PRI] = {};
+      if (prod_cplx())
+        for (int i = 0; i < n.Nc; ++i)
+          for (int k = 0; k < n.cn[i]; ++k)
+            if (n.cnu[i][k] < 0) neg[n.cid[i][k]] = true;
+      for (int r = 0; r < n.Nsr; ++r)
+        if (prod_srf(r))
+          for (int q = 0; q < n.srn[r]; ++q) {
+            const int k = n.src[r][q];
+            for (int l = 0; l < n.sn[k]; ++l)
+              if (n.snu[k][l] < 0) neg[n.sid[k][l]] = true;
+          }
+      for (int j = 0; j < N; ++j) {
+        o << "  const double a" << j << " = L.m[" << j << "]" << (act() ? " * L.g[" + I(j) + "]" : "") << ";\n";
+        if (neg[j]) o << "  const double ra" << j << " = 1.0 / a" << j << ";\n";
+      }
+    }
     for (int j = 0; j < N; ++j) {
       if (act()) o << "  const double la" << j << " = L.lm[" << j << "] + L.lg[" << j << "];\n";
       else o << "  const double la" << j << " = L.lm[" << j << "];\n";
@@ -242,13 +312,19 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     // where the ionic strength is used, at the then current molalities)
     o << "  double Iacc = 0.0, Csum = 0.0;\n";
     for (int i = 0; i < n.Nc; ++i) {
-      o << "  { double s = L.bc[" << i << "];\n";
-      for (int k = 0; k < n.cn[i]; ++k) {
-        const double nu = n.cnu[i][k];
-        const std::string la = "la" + I(n.cid[i][k]);
-        acc(o, "s", nu, la);
+      if (prod_cplx()) {
+        int8_t ids[PFCHEM_MAX_NNZ];
+        for (int k = 0; k < n.cn[i]; ++k) ids[k] = n.cid[i][k];
+        o << "  { const double c = " << prod_expr("L.bc[" + I(i) + "]", n.cn[i], ids, n.cnu[i]) << ";\n";
+      } else {
+        o << "  { double s = L.bc[" << i << "];\n";
+        for (int k = 0; k < n.cn[i]; ++k) {
+          const double nu = n.cnu[i][k];
+          const std::string la = "la" + I(n.cid[i][k]);
+          acc(o, "s", nu, la);
+        }
+        o << "    const double c = xexp(s);\n";
       }
-      o << "    const double c = xexp(s);\n";
       if (n.cZ2[i] > 0) o << "    Iacc = fma(" << lit(n.cZ2[i]) << ", c, Iacc);\n";
       if (n.use_h2o) o << "    Csum += c;\n";
       for (int k = 0; k < n.cn[i]; ++k) {
@@ -351,7 +427,16 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         if (with_free) acc(o, "s", n.sfs[k], "lf");
         for (int l = 0; l < n.sn[k]; ++l) acc(o, "s", n.snu[k][l], "la" + I(n.sid[k][l]));
       };
-      if (!n.srflag[r]) {
+      if (prod_srf(r)) {
+        o << "  double sumE = 0.0;\n";
+        for (int q = 0; q < ncx; ++q) {
+          const int k = n.src[r][q];
+          o << "  S" << q << " = " << prod_expr("L.bs[" + I(k) + "]", n.sn[k], n.sid[k], n.snu[k])
+            << "; sumE += S" << q << ";\n";
+        }
+        o << "  free = site / (1.0 + sumE);\n";
+        for (int q = 0; q < ncx; ++q) o << "  S" << q << " *= free;\n";
+      } else if (!n.srflag[r]) {
         o << "  double sumE = 0.0;\n";
         for (int q = 0; q < ncx; ++q) {
           lq(q, false);
@@ -375,6 +460,14 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         o << "    if (fabs(dfree) < 1e-12 * fabs(free)) one_more = true;\n  }\n";
       }
       o << "  L.srf[" << r << "] = free;\n";
+      // components of any complex on the site (those the free site depends on)
+      std::vector<int> site_comps;
+      for (int q = 0; q < ncx; ++q) {
+        const int k = n.src[r][q];
+        for (int l = 0; l < n.sn[k]; ++l)
+          if (std::find(site_comps.begin(), site_comps.end(), (int)n.sid[k][l]) == site_comps.end())
+            site_comps.push_back(n.sid[k][l]);
+      }
       o << "  double den = 0.0;\n";
       if (jac) {
         for (int j = 0; j < N; ++j) o << "  double dSx" << j << " = 0.0;\n";
@@ -396,12 +489,25 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         }
         if (jac) {
           o << "  { const double nuS = " << times(n.sfs[k], "S" + I(q)) << " * ifree;\n";
-          for (int l = 0; l < n.sn[k]; ++l) {
-            const int j = n.sid[k][l];
-            o << "    { const double t = (" << times(n.snu[k][l], "S" + I(q)) << " + nuS * dSx" << j
-              << " * iden) * L.v_t;\n";
-            for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
-            o << "    }\n";
+          if (n.jac_exact) {
+            // the free site couples every component on the site
+            for (int j : site_comps) {
+              double nu = 0.0;
+              for (int l = 0; l < n.sn[k]; ++l)
+                if (n.sid[k][l] == j) nu += n.snu[k][l];
+              o << "    { const double t = (" << (nu != 0.0 ? times(nu, "S" + I(q)) + " + " : "") << "nuS * dSx" << j
+                << " * iden) * L.v_t;\n";
+              for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
+              o << "    }\n";
+            }
+          } else {
+            for (int l = 0; l < n.sn[k]; ++l) {
+              const int j = n.sid[k][l];
+              o << "    { const double t = (" << times(n.snu[k][l], "S" + I(q)) << " + nuS * dSx" << j
+                << " * iden) * L.v_t;\n";
+              for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
+              o << "    }\n";
+            }
           }
           o << "  }\n";
         }
@@ -446,10 +552,13 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
           << "] += fabs(v); }\n";
       }
       if (jac) {
-        if (n.has_affpow) o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << " / fabs(aff);\n";
+        // exact Jacobian: signed affinity, no den/1000 factor, nothing where QK is capped
+        if (n.jac_exact) o << "  if (lnQK <= 6.90776) {\n";
+        if (n.has_affpow)
+          o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << (n.jac_exact ? " / aff;\n" : " / fabs(aff);\n");
         else o << "  double dIm_dQK = -(Imc * L.vol) * kr;\n";
         if (gen_aff) o << "  dIm_dQK = dIm_dQK * " << lit(1.0 / sig) << " / QK * (1.0 - aff);\n";
-        o << "  double gq = dIm_dQK * QK * L.den_L;\n";
+        o << (n.jac_exact ? "  double gq = dIm_dQK * QK;\n" : "  double gq = dIm_dQK * QK * L.den_L;\n");
         if (n.mlim[mm] > 0.0) {
           o << "  { const double d2 = 1.0 + (1.0 - aff) * " << lit(1.0 / n.mlim[mm]) << ";\n";
           o << "    gq = gq * (1.0 + QK * " << lit(1.0 / n.mlim[mm]) << " / d2) / d2; }\n";
@@ -460,6 +569,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
           for (int k = 0; k < nz; ++k) acc(o, "  " + J(n.mid[mm][k], j), n.mnu[mm][k], "t");
           o << "  }\n";
         }
+        if (n.jac_exact) o << "  }\n";
       }
       o << "  }\n  }\n";
     }
@@ -727,7 +837,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   Lane L;
   long long cell = -1;
   bool exhausted = false;
-  unsigned long long my_iters = 0, my_alt = 0;
+  unsigned long long my_iters = 0, my_alt = 0, my_trips = 0;
   unsigned my_max = 0, my_bad = 0;
   for (;;) {
     const bool want = (cell < 0) && !exhausted;
@@ -760,6 +870,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       if (__all_sync(full, exhausted)) break;
       continue;
     }
+    ++my_trips;
     if (cell >= 0) {
       int st = newton_step(L, Jb, Eb);
       if (st >= 0) {
@@ -779,6 +890,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   }
   if (lane == 0) {
     atomicAdd(&scr->sum_iter, my_iters);
+    atomicAdd(&scr->newton_trips, my_trips);
     (void)my_alt;
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);

@@ -24,6 +24,7 @@ struct DevNet {
   // options
   int32_t use_log, act_freq, use_h2o, isothermal, resid_kind, accum_mode, max_iter, update_kin;
   int32_t has_temkin, has_minscale, has_affpow, has_h2o_rxn;
+  int32_t jac_exact;  // PFCHEM_JACOBIAN_EXACT
   double max_dlnC, rel_change_tol, res_tol;
   double A, B, Bdot;
   // primaries
@@ -84,6 +85,7 @@ struct DevNet {
   unsigned long long next_cell; /* work-queue head */ \
   unsigned long long sum_iter;                        \
   unsigned long long alt_used;                        \
+  unsigned long long newton_trips; /* warp trips of Newton steps */ \
   unsigned int max_iter;                              \
   unsigned int nonconverged;
 

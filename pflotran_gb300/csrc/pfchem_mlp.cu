@@ -546,5 +546,9 @@ cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, fl
 int surrogate_nfeat() { return kFeat; }
 void surrogate_mark_trained(Surrogate *s, bool t) { s->trained = t; }
 bool surrogate_trained(const Surrogate *s) { return s->trained; }
+// True when surrogate_predict can run on `ncells` cells without allocating.
+bool surrogate_ready(const Surrogate *s, long long ncells) {
+  return s->cap >= std::min(ncells, kChunk) && s->feat_cap >= ncells && s->guess_cap >= ncells;
+}
 
 }  // namespace pfchem

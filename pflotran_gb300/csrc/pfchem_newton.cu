@@ -341,7 +341,14 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
         L.S_[i] += v;
         absS[i] += fabs(v);
       }
-      if (JAC) {
+      if (JAC && n.jac_exact) {
+        // the free site couples every component on the site
+        double t[S::NP];
+        for (int j = 0; j < N; ++j) t[j] = nuS * dSx[j] * iden;
+        for (int l = 0; l < n.sn[k]; ++l) t[n.sid[k][l]] += n.snu[k][l] * Sk[q];
+        for (int p = 0; p < n.sn[k]; ++p)
+          for (int j = 0; j < N; ++j) J[(n.sid[k][p] * N + j) * js] += n.snu[k][p] * (t[j] * L.v_t);
+      } else if (JAC) {
         for (int l = 0; l < n.sn[k]; ++l) {
           const int j = n.sid[k][l];
           const double t = (n.snu[k][l] * Sk[q] + nuS * dSx[j] * iden) * L.v_t;
@@ -385,10 +392,11 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
       L.F[i] += v;
       L.Sc[i] += fabs(v);
     }
-    if (JAC) {
-      double dIm_dQK = n.has_affpow ? -ImV * n.mpow[mm] / fabs(aff) : -(Imc * L.vol) * kr;
+    if (JAC && !(n.jac_exact && lnQK > 6.90776)) {  // exact: a capped QK does not depend on m
+      double dIm_dQK = n.has_affpow ? -ImV * n.mpow[mm] / (n.jac_exact ? aff : fabs(aff)) : -(Imc * L.vol) * kr;
       if (n.has_temkin || n.has_minscale) dIm_dQK = dIm_dQK * (1.0 / sig) / QK * (1.0 - aff);
-      double g = dIm_dQK * QK * L.den_mnrl;  // d/dln m_j of QK is nu_j QK; den*1e-3 as the reference
+      // d/dln m_j of QK is nu_j QK; the reference scales it by den*1e-3
+      double g = dIm_dQK * QK * (n.jac_exact ? 1.0 : L.den_mnrl);
       if (n.mlim[mm] > 0.0) {
         const double d2 = 1.0 + (1.0 - aff) / n.mlim[mm];
         g = g * (1.0 + QK / n.mlim[mm] / d2) / d2;
@@ -647,7 +655,7 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
   Lane<S> L;
   int64_t cell = -1;
   bool exhausted = false;
-  unsigned long long my_iters = 0, my_alt = 0;
+  unsigned long long my_iters = 0, my_alt = 0, my_trips = 0;
   unsigned my_max = 0, my_bad = 0;
   for (;;) {
     const bool want = (cell < 0) && !exhausted;
@@ -681,6 +689,7 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
       if (__all_sync(full, exhausted)) break;
       continue;
     }
+    ++my_trips;
     if (cell >= 0) {
       int st = newton_step(n, L, J, js);
       if (st == -2) {
@@ -712,6 +721,7 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
   }
   if (lane == 0) {
     atomicAdd(&scr->sum_iter, my_iters);
+    atomicAdd(&scr->newton_trips, my_trips);
     atomicAdd(&scr->alt_used, my_alt);
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);

@@ -63,6 +63,9 @@ def load(build_if_missing=True):
     l.pfchem_get_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_set_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_autotune.argtypes = [vp, C.c_double, C.POINTER(abi.Cells)]
+    l.pfchem_reserve.argtypes = [vp, C.c_int64]
+    l.pfchem_react_batch_async.argtypes = [vp, C.c_double, C.POINTER(abi.Cells), vp]
+    l.pfchem_async_stats.argtypes = [vp, C.POINTER(abi.Stats)]
     l.pfchem_check_specialized.argtypes = [C.POINTER(abi.Network), C.POINTER(abi.Options), C.c_int, C.c_char_p,
                                            C.c_size_t]
     _lib = l
@@ -187,6 +190,13 @@ class ReactionStep(WarmStartMixin):
         self._check(self._lib.pfchem_set_network(self._ctx, C.byref(self._net_struct), C.byref(options)),
                     "pfchem_set_network")
 
+    def set_options(self, options):
+        """New CHEMISTRY options for the same network (the trained warm
+        start, if any, is kept)."""
+        self.options = options
+        self._check(self._lib.pfchem_set_network(self._ctx, C.byref(self._net_struct), C.byref(options)),
+                    "pfchem_set_network")
+
     def _check(self, r, what):
         if r < 0:
             msg = self._lib.pfchem_last_error(self._ctx).decode()
@@ -217,6 +227,26 @@ class ReactionStep(WarmStartMixin):
         return self._check(self._lib.pfchem_react_batch_interleaved(self._ctx, dt, ncomp, C.c_void_p(ptr),
                                                                     C.byref(s)),
                            "pfchem_react_batch_interleaved")
+
+    def reserve(self, ncells):
+        """Sizes the device buffers so that react_async allocates nothing."""
+        self._check(self._lib.pfchem_reserve(self._ctx, int(ncells)), "pfchem_reserve")
+
+    def react_async(self, cells, dt, stream):
+        """Enqueues one reaction step of device-resident `cells` on `stream`
+        (a torch.cuda.Stream or a raw cudaStream_t handle) without waiting;
+        capturable into a CUDA graph.  The CellBatch struct is kept alive on
+        the object, since a captured graph holds the pointers it names."""
+        self._async_struct = cells.struct()
+        h = getattr(stream, "cuda_stream", stream)
+        return self._check(self._lib.pfchem_react_batch_async(self._ctx, dt, C.byref(self._async_struct),
+                                                              C.c_void_p(h)), "pfchem_react_batch_async")
+
+    def async_stats(self):
+        """Statistics of the last completed react_async step (synchronise its stream first)."""
+        st = abi.Stats()
+        self._check(self._lib.pfchem_async_stats(self._ctx, C.byref(st)), "pfchem_async_stats")
+        return st
 
     def update_kinetic_state(self, cells, dt):
         """RTUpdateKineticState (device batches only)."""

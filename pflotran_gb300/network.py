@@ -288,6 +288,7 @@ def default_options(**kw) -> abi.Options:
     o.max_relative_change_tolerance = 0.0
     o.max_residual_tolerance = 1e-12
     o.update_kinetic_state = 1
+    o.jacobian = abi.JACOBIAN_REFERENCE
     for k, v in kw.items():
         setattr(o, k, v)
     return o

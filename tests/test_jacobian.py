@@ -1,0 +1,58 @@
+"""The Newton Jacobian (CPU, oracle): the exact option is the derivative of
+RReact's residual; the reference's own Jacobian is not, which is why its
+Newton iteration converges linearly on networks with surface complexation
+and precipitating minerals."""
+import numpy as np
+
+from pflotran_gb300 import abi, workloads
+
+
+def _fd_contraction(oracle, net, opt, cells, dt, k, m):
+    """Spectral radius of I - J^-1 J_fd in ln m (the Newton contraction
+    factor near the root) and the max column-scaled Jacobian error."""
+    ns = net.as_struct()
+    _, J = oracle.newton_system(ns, opt, dt, cells, k, m)
+    N = net.N
+    Jfd = np.zeros((N, N))
+    for j in range(N):
+        h = 1e-6 * m[j]
+        mp, mm = m.copy(), m.copy()
+        mp[j] += h
+        mm[j] -= h
+        Jfd[:, j] = (oracle.newton_system(ns, opt, dt, cells, k, mp)[0] -
+                     oracle.newton_system(ns, opt, dt, cells, k, mm)[0]) / (2 * h)
+    A, B = J * m[None, :], Jfd * m[None, :]
+    rho = np.abs(np.linalg.eigvals(np.linalg.solve(A, B) - np.eye(N))).max()
+    return rho
+
+
+def test_exact_jacobian_is_the_derivative(oracle):
+    net, opt, cells, dt = workloads.synthetic_cells(40, seed=21)
+    sol = cells.copy()
+    oracle.react(net.as_struct(), opt, dt, sol, 0, 4)
+    exact = workloads.default_options(use_isothermal=1, jacobian=abi.JACOBIAN_EXACT)
+    rho_ref, rho_exact = [], []
+    for k in range(cells.ncells):
+        if sol.status[k] != 0:
+            continue
+        m = sol.pri_molal.reshape(net.N, -1)[:, k].copy()
+        rho_ref.append(_fd_contraction(oracle, net, opt, cells, dt, k, m))
+        rho_exact.append(_fd_contraction(oracle, net, exact, cells, dt, k, m))
+    rho_ref, rho_exact = np.array(rho_ref), np.array(rho_exact)
+    assert rho_exact.max() < 1e-5, rho_exact.max()          # finite-difference noise only
+    assert np.median(rho_ref) > 1e-3 and rho_ref.max() > 0.1  # linear convergence
+
+
+def test_exact_jacobian_same_root_fewer_iterations(oracle):
+    net, opt, cells, dt = workloads.synthetic_cells(1000, seed=22)
+    a, b = cells.copy(), cells.copy()
+    oracle.react(net.as_struct(), opt, dt, a, 0, 4)
+    exact = workloads.default_options(use_isothermal=1, jacobian=abi.JACOBIAN_EXACT)
+    oracle.react(net.as_struct(), exact, dt, b, 0, 4)
+    ok = (a.status == 0) & (b.status == 0)
+    assert ok.mean() > 0.99
+    rel = np.abs(b.pri_molal - a.pri_molal) / a.pri_molal
+    assert np.percentile(rel.reshape(net.N, -1)[:, ok].max(0), 99) < 1e-10
+    assert rel.reshape(net.N, -1)[:, ok].max() < 1e-8
+    assert b.iterations[ok].mean() < 0.75 * a.iterations[ok].mean()
+    assert b.iterations.max() < 200

@@ -56,3 +56,25 @@ def test_rsolve_reports_singular_row(oracle):
     r = np.ones(3)
     c = np.ones(3)
     assert oracle.lib().pfo_rsolve(3, r.ctypes.data, A.ctypes.data, c.ctypes.data, 0, u.ctypes.data) == 1
+
+
+def test_alternative_guess_choice(oracle):
+    """The two-guess start: the converged solution offered as the second
+    guess is taken and needs one iteration; an invalid second guess leaves
+    the plain solve unchanged bit for bit."""
+    from pflotran_gb300 import workloads
+    net, opt, cells, dt = workloads.calcite_cells(64, seed=3)
+    plain = cells.copy()
+    oracle.react(net.as_struct(), opt, dt, plain, 0, 4)
+    assert (plain.status == 0).all()
+    warm = cells.copy()
+    warm.alt_guess = plain.pri_molal.copy()
+    oracle.react(net.as_struct(), opt, dt, warm, 0, 4)
+    assert (warm.status == 0).all()
+    assert (warm.iterations == 1).all()
+    assert np.array_equal(warm.pri_molal, plain.pri_molal)
+    bad = cells.copy()
+    bad.alt_guess = -np.ones_like(cells.pri_molal)
+    oracle.react(net.as_struct(), opt, dt, bad, 0, 4)
+    assert np.array_equal(bad.pri_molal, plain.pri_molal)
+    assert np.array_equal(bad.iterations, plain.iterations)

@@ -235,3 +235,36 @@ def test_specialized_kernel_is_default():
     net, opt, cells, dt = workloads.calcite_cells(16, seed=14)
     step = ReactionStep(net, opt)
     assert step.launch().variant == abi.KERNEL_SPECIALIZED
+
+
+@pytest.mark.parametrize("variant", [abi.KERNEL_SPECIALIZED, abi.KERNEL_GENERIC])
+def test_exact_jacobian(oracle, variant):
+    """The exact-Jacobian option against the oracle with the same option (same
+    Newton path), and against the reference Jacobian (same equations and
+    root): the answers agree to what the 1e-12 relative residual allows and
+    the exact Jacobian needs fewer iterations."""
+    net, opt, cells, dt = workloads.synthetic_cells(4096, seed=17)
+    opt.jacobian = abi.JACOBIAN_EXACT
+    ref = cells.copy()
+    ref.sec_molal = np.zeros(net.Nc * cells.ncells)
+    d = ref.copy().to_device()
+    oracle.react(net.as_struct(), opt, dt, ref, 0, 8)
+    step = ReactionStep(net, opt)
+    if variant == abi.KERNEL_GENERIC:
+        step.set_launch(64, 1, 8, variant=abi.KERNEL_GENERIC)
+    step.react(d, dt)
+    g = d.to_host()
+    ok = (ref.status == 0) & (g.status == 0)
+    assert ok.mean() > 0.999
+    assert_parity(net, g, ref, mask=ok)
+    assert np.mean(g.iterations == ref.iterations) > 0.98
+    # against the reference Jacobian
+    opt_ref = default_options(use_isothermal=1)
+    base = cells.copy()
+    base.sec_molal = np.zeros(net.Nc * cells.ncells)
+    oracle.react(net.as_struct(), opt_ref, dt, base, 0, 8)
+    both = ok & (base.status == 0)
+    errs = compare(net, g, base, mask=both)
+    assert errs["total"] <= 1e-10 and errs["mnrl_rate"] <= 1e-10 and errs["mnrl_volfrac"] <= 1e-10, errs
+    assert errs["pri_molal"] <= 1e-8, errs
+    assert g.iterations[both].mean() < 0.8 * base.iterations[both].mean()

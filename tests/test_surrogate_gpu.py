@@ -78,14 +78,16 @@ def test_trained_warm_start_reduces_iterations_with_identical_results(oracle):
     ok = (gp.status == 0) & (gw.status == 0)
     rel = np.abs(gw.pri_molal - gp.pri_molal) / gp.pri_molal
     assert rel.reshape(net.N, -1)[:, ok].max() < 1e-8
-    # the warm-started path against the oracle started from the same guess
+    # the warm-started path against the oracle given the same two guesses:
+    # the oracle applies the same choice (residual norm at both) and Newton
     sub_idx = np.arange(4096)
     ref = cells.subset(sub_idx, net)
-    ref.pri_molal = np.ascontiguousarray(pred.reshape(net.N, -1)[:, sub_idx]).ravel()
+    ref.alt_guess = np.ascontiguousarray(pred.reshape(net.N, -1)[:, sub_idx]).ravel()
     ref.sec_molal = np.zeros(net.Nc * len(sub_idx))
     oracle.react(net.as_struct(), opt, dt, ref, 0, 8)
     g_sub = gw.subset(sub_idx, net)
-    same = (ref.status == 0) & (g_sub.status == 0) & (ref.iterations == g_sub.iterations)
-    assert same.mean() > 0.8
-    errs = compare(net, g_sub, ref, mask=same)
+    ok = (ref.status == 0) & (g_sub.status == 0)
+    assert ok.mean() > 0.95
+    assert (ref.iterations == g_sub.iterations)[ok].mean() > 0.98
+    errs = compare(net, g_sub, ref, mask=ok)
     assert all(v <= 1e-10 for v in errs.values()), errs

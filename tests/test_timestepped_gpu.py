@@ -1,0 +1,57 @@
+"""Time-stepped operator-split run on the GPU: transport stand-in + reaction
+step captured in one CUDA graph per step, checked against the oracle on
+sampled cells every step."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle_fn(oracle):
+    return lambda net, opt, dt, cells: oracle.react(net, opt, dt, cells, 0, os.cpu_count() or 1)
+
+
+def test_graph_step_matches_eager_step_bit_for_bit():
+    from pflotran_gb300.os_run import OperatorSplitRun
+    kw = dict(shape=(24, 16, 16), warm_start=False, autotune=False, drift_sample=64, log=None)
+    a = OperatorSplitRun(**kw)
+    b = OperatorSplitRun(**kw)
+    a.run(steps=3)
+    b.run_eager(steps=3)
+    for f in ("total", "pri_molal", "total_out", "mnrl_volfrac", "mnrl_rate", "total_sorb_eq", "iterations"):
+        x, y = getattr(a.cells, f), getattr(b.cells, f)
+        assert bool((x == y).all()), f
+
+
+@pytest.mark.parametrize("warm", [False, True])
+def test_timestepped_drift_against_oracle(oracle, warm):
+    from pflotran_gb300.os_run import OperatorSplitRun
+    run = OperatorSplitRun(shape=(32, 16, 16), warm_start=warm, train_samples=131072, epochs=4, autotune=False,
+                           drift_sample=256, log=None)
+    recs = run.run(steps=4, oracle_fn=_oracle_fn(oracle))
+    for r in recs:
+        assert r["nonconverged"] == 0
+        d = r["drift"]
+        assert d["cells"] == 256
+        assert d["same_iterations"] > 0.98
+        for k in ("pri_molal", "total", "mnrl_rate", "mnrl_volfrac"):
+            assert d[k] <= 1e-10, (r["step"], k, d[k])
+    if warm:
+        assert sum(r["warm_start_used"] for r in recs) > 0
+
+
+@pytest.mark.skipif(not os.environ.get("PFCHEM_TIMESTEPPED_FULL"), reason="full 128^3 x 50-step run on request")
+def test_timestepped_full_size(oracle):
+    """128^3 cells, 50 steps of 1 day, warm start, autotuned: per-step
+    solves/s, iteration histograms and drift (report to the path in
+    PFCHEM_TIMESTEPPED_FULL)."""
+    from pflotran_gb300.os_run import OperatorSplitRun
+    run = OperatorSplitRun(shape=(128, 128, 128), warm_start=True, autotune=True, drift_sample=512)
+    recs = run.run(steps=50, oracle_fn=_oracle_fn(oracle))
+    with open(os.environ["PFCHEM_TIMESTEPPED_FULL"], "w") as f:
+        json.dump({"setup": run.report, "steps": recs}, f)
+    worst = max(max(r["drift"][k] for k in ("pri_molal", "total", "mnrl_rate", "mnrl_volfrac")) for r in recs)
+    assert worst <= 1e-10, worst
