@@ -173,11 +173,12 @@ typedef struct pfchem_options {
  *  - RTotalSorbEqSurfCplx1 adds the free-site part of dS_k/dm_j only for the
  *    components j of complex k (reaction_surf_complex.F90:905-931), although
  *    the free-site concentration depends on every component on the site;
- *  - RKineticMineral divides by |affinity| where the derivative has the
- *    signed affinity (reaction_mineral.F90:842-846), so the mineral term has
- *    the wrong sign for a precipitating mineral, and
- *  - it scales dQK/dm by den_kg/1000 (reaction_mineral.F90:867,885), and
- *    keeps dQK/dm where QK is capped at 1e3 (reaction_mineral.F90:699-703).
+ *  - RKineticMineral keeps dQK/dm where QK is capped at 1e3, so a strongly
+ *    supersaturated mineral contributes a derivative its rate does not have
+ *    (reaction_mineral.F90:699-703, :860-872), scales dQK/dm by den_kg/1000
+ *    (:867, :885), and, when kinmnrl_affinity_power is given, divides by
+ *    |affinity| where the derivative has the signed affinity (:842-846),
+ *    which flips the term's sign for a precipitating mineral.
  * EXACT (no counterpart in the reference) uses the derivatives of the same
  * residual: same equations, same root, fewer iterations; the rate-limiter
  * branch keeps the reference's expression apart from the affinity sign. */

@@ -105,8 +105,16 @@ struct Gen {
     }
     return true;
   }
+  bool prod_mnrl() const {
+    if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) return false;
+    for (int m = 0; m < n.Nm; ++m)
+      for (int k = 0; k < n.mn[m]; ++k)
+        if (!small_int(n.mnu[m][k])) return false;
+    return true;
+  }
   bool prod_any() const {
     if (prod_cplx() && n.Nc > 0) return true;
+    if (prod_mnrl() && n.Nm > 0) return true;
     for (int r = 0; r < n.Nsr; ++r)
       if (prod_srf(r)) return true;
     return false;
@@ -264,6 +272,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       for (int i = 0; i < n.Nc; ++i) o << "  L.bc[" << i << "] = " << bK(i) << ";\n";
     }
     // product-form constants: exp of the log constants, once per cell
+    if (prod_mnrl())
+      for (int k = 0; k < n.Nm; ++k) o << "  L.bm[" << k << "] = xexp(L.bm[" << k << "]);\n";
     if (prod_cplx())
       for (int i = 0; i < n.Nc; ++i) o << "  L.bc[" << i << "] = xexp(L.bc[" << i << "]);\n";
     for (int r = 0; r < n.Nsr; ++r)
@@ -292,6 +302,10 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
             for (int l = 0; l < n.sn[k]; ++l)
               if (n.snu[k][l] < 0) neg[n.sid[k][l]] = true;
           }
+      if (prod_mnrl())
+        for (int m = 0; m < n.Nm; ++m)
+          for (int k = 0; k < n.mn[m]; ++k)
+            if (n.mnu[m][k] < 0) neg[n.mid[m][k]] = true;
       for (int j = 0; j < N; ++j) {
         o << "  const double a" << j << " = L.m[" << j << "]" << (act() ? " * L.g[" + I(j) + "]" : "") << ";\n";
         if (neg[j]) o << "  const double ra" << j << " = 1.0 / a" << j << ";\n";
@@ -527,9 +541,18 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     // kinetic minerals (RKineticMineral)
     for (int mm = 0; mm < n.Nm; ++mm) {
       const int nz = n.mn[mm];
-      o << "  { // mineral " << mm << "\n  double lnQK = L.bm[" << mm << "];\n";
-      for (int k = 0; k < nz; ++k) acc(o, "lnQK", n.mnu[mm][k], "la" + I(n.mid[mm][k]));
-      o << "  const double QK = (lnQK <= 6.90776) ? xexp(lnQK) : 1e3;\n";
+      // the cap of RKineticMineral (QK = 1e3 where ln QK > 6.90776) becomes,
+      // in product form, a comparison of QK itself with exp(6.90776)
+      const std::string qk_ok = prod_mnrl() ? "(QKp <= " + lit(std::exp(6.90776)) + ")" : "(lnQK <= 6.90776)";
+      if (prod_mnrl()) {
+        o << "  { // mineral " << mm << "\n  const double QKp = "
+          << prod_expr("L.bm[" + I(mm) + "]", nz, n.mid[mm], n.mnu[mm]) << ";\n";
+        o << "  const double QK = " << qk_ok << " ? QKp : 1e3;\n";
+      } else {
+        o << "  { // mineral " << mm << "\n  double lnQK = L.bm[" << mm << "];\n";
+        for (int k = 0; k < nz; ++k) acc(o, "lnQK", n.mnu[mm][k], "la" + I(n.mid[mm][k]));
+        o << "  const double QK = " << qk_ok << " ? xexp(lnQK) : 1e3;\n";
+      }
       double sig = 1.0;
       if (n.has_temkin) sig = n.mtemkin[mm];
       if (n.has_minscale) sig *= n.mscale[mm];
@@ -553,7 +576,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       }
       if (jac) {
         // exact Jacobian: signed affinity, no den/1000 factor, nothing where QK is capped
-        if (n.jac_exact) o << "  if (lnQK <= 6.90776) {\n";
+        if (n.jac_exact) o << "  if " << qk_ok << " {\n";
         if (n.has_affpow)
           o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << (n.jac_exact ? " / aff;\n" : " / fabs(aff);\n");
         else o << "  double dIm_dQK = -(Imc * L.vol) * kr;\n";
@@ -717,14 +740,25 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       o << "  sum += L.m[" << j << "];\n";
     }
     o << "  if (a.sec_molal) {\n";
-    for (int j = 0; j < n.N; ++j) {
-      if (act()) o << "  const double la" << j << " = L.lm[" << j << "] + L.lg[" << j << "];\n";
-      else o << "  const double la" << j << " = L.lm[" << j << "];\n";
-    }
-    for (int i = 0; i < n.Nc; ++i) {
-      o << "  { double s = L.bc[" << i << "];\n";
-      for (int k = 0; k < n.cn[i]; ++k) acc(o, "s", n.cnu[i][k], "la" + I(n.cid[i][k]));
-      o << "    a.sec_molal[" << i << " * nc + cell] = exp(s); }\n";
+    if (prod_cplx()) {
+      // L.bc holds the product-form constants
+      for (int j = 0; j < n.N; ++j) {
+        o << "  const double a" << j << " = L.m[" << j << "]" << (act() ? " * L.g[" + I(j) + "]" : "") << ";\n";
+        o << "  const double ra" << j << " = 1.0 / a" << j << ";\n";
+      }
+      for (int i = 0; i < n.Nc; ++i)
+        o << "  a.sec_molal[" << i << " * nc + cell] = " << prod_expr("L.bc[" + I(i) + "]", n.cn[i], n.cid[i], n.cnu[i])
+          << ";\n";
+    } else {
+      for (int j = 0; j < n.N; ++j) {
+        if (act()) o << "  const double la" << j << " = L.lm[" << j << "] + L.lg[" << j << "];\n";
+        else o << "  const double la" << j << " = L.lm[" << j << "];\n";
+      }
+      for (int i = 0; i < n.Nc; ++i) {
+        o << "  { double s = L.bc[" << i << "];\n";
+        for (int k = 0; k < n.cn[i]; ++k) acc(o, "s", n.cnu[i][k], "la" + I(n.cid[i][k]));
+        o << "    a.sec_molal[" << i << " * nc + cell] = exp(s); }\n";
+      }
     }
     o << "  }\n";
     o << "  sum += L.Csum;\n";

@@ -46,4 +46,8 @@ def compare(net, gpu, ref, tol=1e-10, mask=None):
         s = np.maximum(np.abs(r).sum(0, keepdims=True) * 1e-6, 1e-300)
         out["total_sorb_eq"] = rel_err(g, r, s)[:, mask].max()
     out["ionic_strength"] = rel_err(gpu.ionic_strength, ref.ionic_strength, 0.0)[mask].max()
+    if net.Nc and gpu.sec_molal is not None and ref.sec_molal is not None:
+        # complexes below 1e-280 mol/kg are noise next to any total
+        out["sec_molal"] = rel_err(gpu.sec_molal.reshape(-1, n)[:net.Nc], ref.sec_molal.reshape(-1, n)[:net.Nc],
+                                   1e-280)[:, mask].max()
     return out
