@@ -290,6 +290,57 @@ int pfchem_reserve(pfchem_ctx *ctx, int64_t ncells);
 int pfchem_react_batch_async(pfchem_ctx *ctx, double dt, pfchem_cells *cells, void *stream);
 int pfchem_async_stats(pfchem_ctx *ctx, pfchem_stats *stats);
 
+/* Per-cell blocks of the global-implicit transport system (the path PFLOTRAN
+ * runs when operator splitting is off): the reaction residual and its
+ * Jacobian that RTResidual and RTJacobian add cell by cell
+ * (reactive_transport.F90:2729-2760, :3440-3468) through RReaction /
+ * RReactionDerivative (reaction.F90:3515-3686, analytical derivatives), and
+ * the auxiliary totals and their derivatives from RTAuxVarCompute
+ * (reaction.F90:4969-5068) that the accumulation blocks are built from.
+ * Evaluated at each cell's current pri_molal with log K at the cell
+ * temperature and LAG activity coefficients at cells->ionic_strength.  Device
+ * pointers; cells->total is not read.  Blocks are naqcomp x naqcomp per cell,
+ * column-major as the Fortran Jac(ncomp,ncomp) that MatSetValuesBlockedLocal
+ * receives: element (i,j) of cell c at [c*N*N + j*N + i].  Inactive cells get
+ * zero blocks.  The ion-exchange and surface free-site warm starts are
+ * updated; mnrl_rate, sec_molal and status are written when given. */
+typedef struct pfchem_reaction_blocks_out {
+  double *res;          /* (naqcomp, ncells) RReaction residual [mol/s]                */
+  double *jac;          /* blocks: dRes_i/dm_j [kg water/s]                            */
+  double *total;        /* (naqcomp, ncells) aqueous totals [mol/L], or NULL            */
+  double *dtotal;       /* blocks: d total_i / d m_j [kg water/L], or NULL              */
+  double *total_sorb;   /* (naqcomp, ncells) sorbed totals [mol/m^3 bulk], or NULL      */
+  double *dtotal_sorb;  /* blocks: d total_sorb_i / d m_j [kg water/m^3 bulk], or NULL  */
+} pfchem_reaction_blocks_out;
+int pfchem_reaction_blocks(pfchem_ctx *ctx, pfchem_cells *cells, pfchem_reaction_blocks_out *out);
+
+/* Mineral-driven porosity and surface-area update after the kinetic state
+ * (RealizationUpdatePropertiesTS, realization_subsurface.F90:1686-1735, and
+ * RealizationCalcMineralPorosity, :1946-2001):
+ *   porosity = max(1 - sum_m phi_m, minimum_porosity)          (update_porosity)
+ *   area_m   = area0_m * (porosity/porosity0)^p_por,m * (phi_m/phi0_m)^p_vf,m
+ * with the porosity factor only when surface_area_with_porosity and the
+ * volume-fraction factor only where phi0_m > 0.  All cells, active or not,
+ * as the reference.  The mineral-armoring branch (:1737-1765) is not
+ * supported: it carries a flag from cell to cell, so its result depends on
+ * the cell order.  Device pointers. */
+typedef struct pfchem_mineral_update {
+  int32_t update_porosity;             /* reaction%update_porosity                       */
+  int32_t update_surface_area;         /* reaction%update_mineral_surface_area           */
+  int32_t surface_area_with_porosity;  /* reaction%update_mnrl_surf_with_porosity        */
+  int32_t reserved;
+  double minimum_porosity;             /* reaction%minimum_porosity                      */
+  const double *surf_area_vol_frac_pwr;/* (nkinmnrl) kinmnrl_surf_area_vol_frac_pwr      */
+  const double *surf_area_porosity_pwr;/* (nkinmnrl) kinmnrl_surf_area_porosity_pwr, or NULL */
+  const double *mnrl_volfrac0;         /* (nkinmnrl, ncells) rt_auxvar%mnrl_volfrac0     */
+  const double *mnrl_area0;            /* (nkinmnrl, ncells) rt_auxvar%mnrl_area0        */
+  const double *porosity0;             /* (ncells) field%porosity0, or NULL without the porosity factor */
+  double *porosity;                    /* (ncells) out: porosity_base when update_porosity, else NULL */
+} pfchem_mineral_update;
+/* Reads cells->mnrl_volfrac (and cells->porosity when porosity is not
+ * updated), writes cells->mnrl_area and mu->porosity. */
+int pfchem_update_mineral_properties(pfchem_ctx *ctx, pfchem_cells *cells, const pfchem_mineral_update *mu);
+
 /* Statistics of the last react call: what the OS_STATISTICS block of RTReact
  * accumulates (reactive_transport.F90:1645-1804). */
 int pfchem_last_stats(const pfchem_ctx *ctx, pfchem_stats *stats);

@@ -37,6 +37,8 @@ def lib():
         l.pfo_interpolate_logK.argtypes = [C.c_void_p, C.c_double]
         l.pfo_interpolate_logK.restype = C.c_double
         l.pfo_ifc67_density.argtypes = [C.c_double, C.c_double]
+        l.pfo_update_mineral_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        l.pfo_reaction_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         l.pfo_newton_system.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_int64, C.c_void_p,
                                         C.c_void_p, C.c_void_p]
         l.pfo_ifc67_density.restype = C.c_double
@@ -112,3 +114,26 @@ def newton_system(net_struct, opt, dt, cells, k, m):
     if r:
         raise RuntimeError("pfo_newton_system failed")
     return F, J.reshape(N, N)
+
+
+def reaction_blocks(net_struct, opt, cells):
+    """Global-implicit per-cell blocks of a host CellBatch (see pfo_reaction_blocks):
+    dict of numpy arrays shaped like ReactionStep.reaction_blocks'."""
+    import numpy as np
+    from pflotran_gb300 import abi
+    n = cells.ncells
+    N = cells.pri_molal.size // n
+    out = {"res": np.zeros((N, n)), "total": np.zeros((N, n)), "total_sorb": np.zeros((N, n)),
+           "jac": np.zeros((n, N, N)), "dtotal": np.zeros((n, N, N)), "dtotal_sorb": np.zeros((n, N, N))}
+    o = abi.ReactionBlocksOut(*[out[k].ctypes.data for k in ("res", "jac", "total", "dtotal", "total_sorb",
+                                                             "dtotal_sorb")])
+    s = cells.struct()
+    if lib().pfo_reaction_blocks(C.byref(net_struct), C.byref(opt), C.byref(s), C.byref(o)):
+        raise RuntimeError("pfo_reaction_blocks failed")
+    return out
+
+
+def update_mineral_properties(net_struct, cells, mu):
+    """Restated porosity / mineral surface-area update on a host CellBatch."""
+    s = cells.struct()
+    return lib().pfo_update_mineral_properties(C.byref(net_struct), C.byref(s), C.byref(mu))

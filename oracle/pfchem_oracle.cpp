@@ -1221,6 +1221,96 @@ int pfo_newton_system(const pfchem_network *net, const pfchem_options *opt, doub
   return 0;
 }
 
+// Global-implicit per-cell blocks (RTResidual/RTJacobian reaction terms,
+// reactive_transport.F90:2729-2760, :3440-3468): RTAuxVarCompute at the
+// cell's pri_molal (totals, sorbed totals and their derivatives,
+// reaction.F90:4969-5068) and RReaction with analytical derivative
+// (reaction.F90:3515-3584, 3588-3616), log K at the cell temperature, LAG
+// activity coefficients at the cell's ionic strength.  Blocks are
+// column-major per cell (Fortran Jac(ncomp,ncomp)).
+int pfo_reaction_blocks(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
+                        pfchem_reaction_blocks_out *out) {
+  Net w = make_net(net, opt);
+  const pfchem_options &o = *opt;
+  const int N = w.N;
+  const int64_t n = cells->ncells, NN = (int64_t)N * N;
+  for (int64_t k = 0; k < n; ++k) {
+    if (cells->active && cells->active[k] <= 0) {
+      for (int j = 0; j < N; ++j) {
+        out->res[j * n + k] = 0.0;
+        if (out->total) out->total[j * n + k] = 0.0;
+        if (out->total_sorb) out->total_sorb[j * n + k] = 0.0;
+      }
+      for (int64_t q = 0; q < NN; ++q) {
+        out->jac[k * NN + q] = 0.0;
+        if (out->dtotal) out->dtotal[k * NN + q] = 0.0;
+        if (out->dtotal_sorb) out->dtotal_sorb[k * NN + q] = 0.0;
+      }
+      if (cells->status) cells->status[k] = PFCHEM_CELL_INACTIVE;
+      continue;
+    }
+    Cell<double> c;
+    load_cell(w, cells, k, c);
+    update_temp_dependent_coefs(w, o, c);
+    if (o.act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF)
+      activity_coefficients(w, o, c, true, cells->ionic_strength[k]);
+    int status = auxvar_compute(w, c) ? PFCHEM_CELL_INNER_MAXITER : PFCHEM_CELL_CONVERGED;
+    double Res[P], Jac[P][P];
+    for (int i = 0; i < N; ++i) {
+      Res[i] = 0.0;
+      for (int j = 0; j < N; ++j) Jac[i][j] = 0.0;
+    }
+    if (w.Nm > 0) kinetic_mineral(w, c, Res, Jac, true);
+    const bool sorb = w.Nix + w.Nsr > 0;
+    for (int i = 0; i < N; ++i) {
+      out->res[i * n + k] = Res[i];
+      if (out->total) out->total[i * n + k] = c.total[i];
+      if (out->total_sorb) out->total_sorb[i * n + k] = sorb ? c.total_sorb_eq[i] : 0.0;
+      for (int j = 0; j < N; ++j) {
+        out->jac[k * NN + j * N + i] = Jac[i][j];
+        if (out->dtotal) out->dtotal[k * NN + j * N + i] = c.dtotal[i][j];
+        if (out->dtotal_sorb) out->dtotal_sorb[k * NN + j * N + i] = sorb ? c.dtotal_sorb_eq[i][j] : 0.0;
+      }
+    }
+    for (int m = 0; m < w.Nm; ++m)
+      if (cells->mnrl_rate) cells->mnrl_rate[m * n + k] = c.mnrl_rate[m];
+    for (int i = 0; i < w.Nc; ++i)
+      if (cells->sec_molal) cells->sec_molal[i * n + k] = c.sec_molal[i];
+    for (int r = 0; r < w.Nix; ++r) cells->eqionx_ref_cation_sorbed_conc[r * n + k] = c.eqionx_ref_cation_sorbed_conc[r];
+    for (int r = 0; r < w.Nsr; ++r) cells->srfcplxrxn_free_site_conc[r * n + k] = c.srfcplxrxn_free_site_conc[r];
+    if (cells->status) cells->status[k] = status;
+  }
+  return 0;
+}
+
+// realization_subsurface.F90:1686-1735 (mineral surface area) and
+// :1946-2001 (RealizationCalcMineralPorosity), over all cells.
+int pfo_update_mineral_properties(const pfchem_network *net, pfchem_cells *cells, const pfchem_mineral_update *mu) {
+  const int Nm = net->nkinmnrl;
+  const int64_t n = cells->ncells;
+  for (int64_t k = 0; k < n; ++k) {
+    double por = cells->porosity[k];
+    if (mu->update_porosity && Nm > 0) {
+      double sum_volfrac = 0.0;
+      for (int m = 0; m < Nm; ++m) sum_volfrac = sum_volfrac + cells->mnrl_volfrac[m * n + k];
+      por = std::max(1.0 - sum_volfrac, mu->minimum_porosity);
+      mu->porosity[k] = por;
+    }
+    if (!mu->update_surface_area) continue;
+    for (int m = 0; m < Nm; ++m) {
+      double porosity_scale = 1.0;
+      if (mu->surface_area_with_porosity)
+        porosity_scale = std::pow(por / mu->porosity0[k], mu->surf_area_porosity_pwr[m]);
+      double volfrac_scale = 1.0;
+      if (mu->mnrl_volfrac0[m * n + k] > 0.0)
+        volfrac_scale = std::pow(cells->mnrl_volfrac[m * n + k] / mu->mnrl_volfrac0[m * n + k],
+                                 mu->surf_area_vol_frac_pwr[m]);
+      cells->mnrl_area[m * n + k] = mu->mnrl_area0[m * n + k] * porosity_scale * volfrac_scale;
+    }
+  }
+  return 0;
+}
+
 int pfo_speciate(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells) {
   Net w = make_net(net, opt);
   const int64_t n = cells->ncells;

@@ -127,3 +127,32 @@ CELL_FIELDS_IN = ("temperature", "saturation", "den_kg", "porosity", "volume",
 CELL_FIELDS_STATE = ("pri_molal", "ionic_strength", "ln_act_h2o", "mnrl_volfrac", "mnrl_area",
                      "total_sorb_eq", "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc")
 CELL_FIELDS_OUT = ("total_out", "mnrl_rate", "sec_molal", "iterations", "status", "alt_guess")
+
+
+class ReactionBlocksOut(C.Structure):
+    """pfchem_reaction_blocks_out."""
+    _fields_ = [("res", C.c_void_p), ("jac", C.c_void_p), ("total", C.c_void_p), ("dtotal", C.c_void_p),
+                ("total_sorb", C.c_void_p), ("dtotal_sorb", C.c_void_p)]
+
+
+class MineralUpdate(C.Structure):
+    """pfchem_mineral_update."""
+    _fields_ = [("update_porosity", C.c_int32), ("update_surface_area", C.c_int32),
+                ("surface_area_with_porosity", C.c_int32), ("reserved", C.c_int32),
+                ("minimum_porosity", C.c_double), ("surf_area_vol_frac_pwr", C.c_void_p),
+                ("surf_area_porosity_pwr", C.c_void_p), ("mnrl_volfrac0", C.c_void_p), ("mnrl_area0", C.c_void_p),
+                ("porosity0", C.c_void_p), ("porosity", C.c_void_p)]
+
+
+def mineral_update(arrays, update_porosity=1, update_surface_area=1, surface_area_with_porosity=0,
+                   minimum_porosity=0.0):
+    """MineralUpdate over `arrays` (dict of numpy arrays or torch tensors keyed
+    by the pointer fields); the arrays must stay alive while it is used."""
+    def ptr(k):
+        a = arrays.get(k)
+        if a is None:
+            return None
+        return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
+    return MineralUpdate(update_porosity, update_surface_area, surface_area_with_porosity, 0, minimum_porosity,
+                         ptr("surf_area_vol_frac_pwr"), ptr("surf_area_porosity_pwr"), ptr("mnrl_volfrac0"),
+                         ptr("mnrl_area0"), ptr("porosity0"), ptr("porosity"))

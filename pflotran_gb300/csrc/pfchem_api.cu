@@ -23,6 +23,9 @@ namespace pfchem {
 cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
                          cudaStream_t st);
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
+cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, cudaStream_t st);
+cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
+                                   double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
 int gen_kernel(const DevNet &n, int block, void **fn_out, void **pro_out, std::string *err);
 int gen_prep_fields(const DevNet &n);
@@ -692,6 +695,44 @@ int pfchem_async_stats(pfchem_ctx *c, pfchem_stats *s) {
   s->alt_guess_used = (int64_t)h.alt_used;
   s->kernel_ms = 0.0;
   s->lane_slots = 32 * (int64_t)h.newton_trips;
+  return 0;
+}
+
+int pfchem_reaction_blocks(pfchem_ctx *c, pfchem_cells *cl, pfchem_reaction_blocks_out *out) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device) return fail(c, -1, "pfchem_reaction_blocks takes device pointers");
+  if (!out || !out->res || !out->jac) return fail(c, -1, "res and jac are required");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  cudaError_t le = launch_reaction_blocks(c->net, a, out->res, out->jac, out->total, out->dtotal, out->total_sorb,
+                                          out->dtotal_sorb, c->stream);
+  if (le != cudaSuccess) return fail(c, -2, "reaction-blocks launch: %s", cudaGetErrorString(le));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int pfchem_update_mineral_properties(pfchem_ctx *c, pfchem_cells *cl, const pfchem_mineral_update *mu) {
+  if (!c || !cl || !mu) return fail(c, -1, "null argument");
+  if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
+  if (!cl->on_device) return fail(c, -1, "pfchem_update_mineral_properties takes device pointers");
+  const int Nm = c->net.Nm;
+  if (Nm > 0 && (!cl->mnrl_volfrac || !cl->mnrl_area)) return fail(c, -1, "mnrl_volfrac/mnrl_area required");
+  if (!cl->porosity) return fail(c, -1, "porosity required");
+  if (mu->update_porosity && Nm > 0 && !mu->porosity) return fail(c, -1, "porosity output required");
+  if (mu->update_surface_area && Nm > 0) {
+    if (!mu->surf_area_vol_frac_pwr || !mu->mnrl_volfrac0 || !mu->mnrl_area0)
+      return fail(c, -1, "surf_area_vol_frac_pwr, mnrl_volfrac0 and mnrl_area0 required");
+    if (mu->surface_area_with_porosity && (!mu->surf_area_porosity_pwr || !mu->porosity0))
+      return fail(c, -1, "surf_area_porosity_pwr and porosity0 required with surface_area_with_porosity");
+  }
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  cudaError_t le = launch_mineral_properties(a, Nm, *mu, c->stream);
+  if (le != cudaSuccess) return fail(c, -2, "mineral-properties launch: %s", cudaGetErrorString(le));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return 0;
 }
 

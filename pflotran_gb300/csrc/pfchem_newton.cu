@@ -54,6 +54,7 @@ template <class S>
 struct Lane {
   // per-cell constants of the step
   double dt, acc, psv_den, jac_aq, vol, v_t, den_L, den_mnrl, temp, por, rho_s, lnaw;
+  double jac_mnrl;  // weight of the mineral terms in the Jacobian (1 in the Newton solve)
   // state
   double m[S::NP], lnm[S::NP], lngp[S::NP], gp[S::NP];
   double fixed[S::NP], absfixed[S::NP];
@@ -111,9 +112,10 @@ __device__ void setup(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> 
   L.jac_aq = psv * inv_dt * L.den_L;
   L.v_t = vol * inv_dt;
   L.lnaw = a.lnaw ? a.lnaw[cell] : 0.0;
+  L.jac_mnrl = 1.0;
   const bool sorb = (n.Nix + n.Nsr) > 0;
   for (int j = 0; j < n.N; ++j) {
-    const double tot = a.total[j * a.total_stride_comp + cell * a.total_stride_cell];
+    const double tot = a.total ? a.total[j * a.total_stride_comp + cell * a.total_stride_cell] : 0.0;
     double f = psv * tot;
     if (sorb) f = f + a.sorb[j * nc + cell] * vol;
     L.fixed[j] = L.acc * f;
@@ -396,7 +398,7 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
       double dIm_dQK = n.has_affpow ? -ImV * n.mpow[mm] / (n.jac_exact ? aff : fabs(aff)) : -(Imc * L.vol) * kr;
       if (n.has_temkin || n.has_minscale) dIm_dQK = dIm_dQK * (1.0 / sig) / QK * (1.0 - aff);
       // d/dln m_j of QK is nu_j QK; the reference scales it by den*1e-3
-      double g = dIm_dQK * QK * (n.jac_exact ? 1.0 : L.den_mnrl);
+      double g = dIm_dQK * QK * (n.jac_exact ? 1.0 : L.den_mnrl) * L.jac_mnrl;
       if (n.mlim[mm] > 0.0) {
         const double d2 = 1.0 + (1.0 - aff) / n.mlim[mm];
         g = g * (1.0 + QK / n.mlim[mm] / d2) / d2;
@@ -838,6 +840,136 @@ __global__ void __launch_bounds__(256) kinetic_state_kernel(const __grid_constan
   }
 }
 
+// Global-implicit blocks: three evaluations at the cell's state, each with
+// the Jacobian weights of one term (aqueous totals, sorbed totals, minerals),
+// written out per cell as column-major d/dm blocks.
+struct BlocksOut {
+  double *res, *jac, *total, *dtotal, *total_sorb, *dtotal_sorb;
+};
+
+template <class S>
+__device__ void store_block(const DevNet &n, const Lane<S> &L, const double *J, int js, double *blk, int64_t cell) {
+  const int N = n.N;
+  double *b = blk + cell * (int64_t)N * N;
+  for (int j = 0; j < N; ++j) {
+    const double im = 1.0 / L.m[j];  // d/dln m -> d/dm
+    for (int i = 0; i < N; ++i) b[j * N + i] = J[(i * N + j) * js] * im;
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(32) reaction_blocks_kernel(const __grid_constant__ DevNet n,
+                                                             const __grid_constant__ CellArgs a, BlocksOut o) {
+  extern __shared__ double smem[];
+  const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (cell >= a.ncells) return;
+  const int N = n.N;
+  const int64_t nc = a.ncells, NN = (int64_t)N * N;
+  double *J = smem + threadIdx.x;
+  const int js = blockDim.x;
+  if (a.active && a.active[cell] <= 0) {
+    for (int j = 0; j < N; ++j) {
+      o.res[j * nc + cell] = 0.0;
+      if (o.total) o.total[j * nc + cell] = 0.0;
+      if (o.total_sorb) o.total_sorb[j * nc + cell] = 0.0;
+    }
+    for (int64_t q = 0; q < NN; ++q) {
+      o.jac[cell * NN + q] = 0.0;
+      if (o.dtotal) o.dtotal[cell * NN + q] = 0.0;
+      if (o.dtotal_sorb) o.dtotal_sorb[cell * NN + q] = 0.0;
+    }
+    if (a.status) a.status[cell] = PFCHEM_CELL_INACTIVE;
+    return;
+  }
+  Lane<S> L;
+  setup(n, a, cell, L, 1.0);
+  L.acc = 0.0;  // no accumulation terms in the residual: F = reaction terms only
+  for (int j = 0; j < N; ++j) L.fixed[j] = L.absfixed[j] = 0.0;
+  int status = 0;
+  // aqueous totals and d total / d ln m (x den/1000, as RTotal returns them)
+  L.jac_aq = L.den_L;
+  L.v_t = 0.0;
+  L.jac_mnrl = 0.0;
+  status |= evaluate<S, true>(n, L, J, js);
+  if (o.total)
+    for (int j = 0; j < N; ++j) o.total[j * nc + cell] = L.Psi[j] * L.den_L;
+  if (o.dtotal) store_block(n, L, J, js, o.dtotal, cell);
+  // sorbed totals and their derivatives
+  if (n.Nix + n.Nsr > 0 && (o.total_sorb || o.dtotal_sorb)) {
+    L.jac_aq = 0.0;
+    L.v_t = 1.0;
+    status |= evaluate<S, true>(n, L, J, js);
+    if (o.total_sorb)
+      for (int j = 0; j < N; ++j) o.total_sorb[j * nc + cell] = L.S_[j];
+    if (o.dtotal_sorb) store_block(n, L, J, js, o.dtotal_sorb, cell);
+  } else {
+    if (o.total_sorb)
+      for (int j = 0; j < N; ++j) o.total_sorb[j * nc + cell] = 0.0;
+    if (o.dtotal_sorb)
+      for (int64_t q = 0; q < NN; ++q) o.dtotal_sorb[cell * NN + q] = 0.0;
+  }
+  // reaction residual (RReaction) and its derivative
+  L.jac_aq = 0.0;
+  L.v_t = 0.0;
+  L.jac_mnrl = 1.0;
+  status |= evaluate<S, true>(n, L, J, js);
+  for (int j = 0; j < N; ++j) o.res[j * nc + cell] = L.F[j];
+  store_block(n, L, J, js, o.jac, cell);
+  for (int k = 0; k < n.Nm; ++k)
+    if (a.rate) a.rate[k * nc + cell] = L.rate[k];
+  for (int i = 0; i < n.Nc; ++i)
+    if (a.sec_molal) a.sec_molal[i * nc + cell] = L.C[i];
+  for (int r = 0; r < n.Nix; ++r) a.ixref[r * nc + cell] = L.ixref[r];
+  for (int r = 0; r < n.Nsr; ++r) a.srfree[r * nc + cell] = L.srfree[r];
+  if (a.status) a.status[cell] = status ? PFCHEM_CELL_INNER_MAXITER : PFCHEM_CELL_CONVERGED;
+}
+
+template <class S>
+static cudaError_t launch_blocks_t(const DevNet &n, const CellArgs &a, const BlocksOut &o, cudaStream_t st) {
+  const int block = 32;
+  const size_t shm = (size_t)n.N * n.N * block * sizeof(double);
+  if (shm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(reaction_blocks_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)shm);
+    if (e != cudaSuccess) return e;
+  }
+  const int64_t grid = (a.ncells + block - 1) / block;
+  reaction_blocks_kernel<S><<<(unsigned)grid, block, shm, st>>>(n, a, o);
+  return cudaGetLastError();
+}
+
+// Mineral-driven porosity and surface area (one thread per cell).
+__global__ void __launch_bounds__(128) mineral_properties_kernel(const __grid_constant__ CellArgs a, int Nm,
+                                                                 pfchem_mineral_update mu) {
+  const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nc = a.ncells;
+  if (cell >= nc) return;
+  double por = a.por[cell];
+  if (mu.update_porosity && Nm > 0) {
+    double sum = 0.0;
+    for (int k = 0; k < Nm; ++k) sum += a.vf[k * nc + cell];
+    por = fmax(1.0 - sum, mu.minimum_porosity);
+    mu.porosity[cell] = por;
+  }
+  if (!mu.update_surface_area) return;
+  const double ratio = mu.surface_area_with_porosity ? por / mu.porosity0[cell] : 1.0;
+  for (int k = 0; k < Nm; ++k) {
+    double ps = 1.0;
+    if (mu.surface_area_with_porosity) ps = pow(ratio, mu.surf_area_porosity_pwr[k]);
+    double vs = 1.0;
+    const double vf0 = mu.mnrl_volfrac0[k * nc + cell];
+    if (vf0 > 0.0) vs = pow(a.vf[k * nc + cell] / vf0, mu.surf_area_vol_frac_pwr[k]);
+    a.area[k * nc + cell] = mu.mnrl_area0[k * nc + cell] * ps * vs;
+  }
+}
+
+cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, cudaStream_t st) {
+  const int block = 128;
+  const int64_t grid = (a.ncells + block - 1) / block;
+  mineral_properties_kernel<<<(unsigned)grid, block, 0, st>>>(a, Nm, mu);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 // launch helpers (host)
 template <class S>
@@ -874,6 +1006,16 @@ cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int g
     case 0: return launch_react_t<SizesS>(n, a, scr, grid, block, refill, st);
     case 1: return launch_react_t<SizesM>(n, a, scr, grid, block, refill, st);
     default: return launch_react_t<SizesL>(n, a, scr, grid, block, refill, st);
+  }
+}
+
+cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
+                                   double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st) {
+  const BlocksOut o{res, jac, total, dtotal, total_sorb, dtotal_sorb};
+  switch (size_class(n)) {
+    case 0: return launch_blocks_t<SizesS>(n, a, o, st);
+    case 1: return launch_blocks_t<SizesM>(n, a, o, st);
+    default: return launch_blocks_t<SizesL>(n, a, o, st);
   }
 }
 

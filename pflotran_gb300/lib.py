@@ -63,6 +63,8 @@ def load(build_if_missing=True):
     l.pfchem_get_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_set_launch.argtypes = [vp, C.POINTER(abi.Launch)]
     l.pfchem_autotune.argtypes = [vp, C.c_double, C.POINTER(abi.Cells)]
+    l.pfchem_reaction_blocks.argtypes = [vp, C.POINTER(abi.Cells), C.POINTER(abi.ReactionBlocksOut)]
+    l.pfchem_update_mineral_properties.argtypes = [vp, C.POINTER(abi.Cells), C.POINTER(abi.MineralUpdate)]
     l.pfchem_reserve.argtypes = [vp, C.c_int64]
     l.pfchem_react_batch_async.argtypes = [vp, C.c_double, C.POINTER(abi.Cells), vp]
     l.pfchem_async_stats.argtypes = [vp, C.POINTER(abi.Stats)]
@@ -247,6 +249,31 @@ class ReactionStep(WarmStartMixin):
         st = abi.Stats()
         self._check(self._lib.pfchem_async_stats(self._ctx, C.byref(st)), "pfchem_async_stats")
         return st
+
+    def reaction_blocks(self, cells):
+        """Global-implicit per-cell blocks at the cells' current state (device
+        batch): dict of device tensors res (N, ncells), jac / dtotal /
+        dtotal_sorb (ncells, N, N) with [c, j, i] = d(.)_i/dm_j, total and
+        total_sorb (N, ncells)."""
+        import torch
+        N, n = self.network.N, cells.ncells
+        out = {"res": torch.empty((N, n), dtype=torch.float64, device="cuda"),
+               "total": torch.empty((N, n), dtype=torch.float64, device="cuda"),
+               "total_sorb": torch.empty((N, n), dtype=torch.float64, device="cuda")}
+        for k in ("jac", "dtotal", "dtotal_sorb"):
+            out[k] = torch.empty((n, N, N), dtype=torch.float64, device="cuda")
+        o = abi.ReactionBlocksOut(*[out[k].data_ptr() for k in ("res", "jac", "total", "dtotal", "total_sorb",
+                                                                  "dtotal_sorb")])
+        s = cells.struct()
+        self._check(self._lib.pfchem_reaction_blocks(self._ctx, C.byref(s), C.byref(o)), "pfchem_reaction_blocks")
+        return out
+
+    def update_mineral_properties(self, cells, mu):
+        """Porosity and mineral surface area from the volume fractions
+        (device batch; `mu` an abi.MineralUpdate over device arrays)."""
+        s = cells.struct()
+        return self._check(self._lib.pfchem_update_mineral_properties(self._ctx, C.byref(s), C.byref(mu)),
+                           "pfchem_update_mineral_properties")
 
     def update_kinetic_state(self, cells, dt):
         """RTUpdateKineticState (device batches only)."""

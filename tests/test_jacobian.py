@@ -56,3 +56,50 @@ def test_exact_jacobian_same_root_fewer_iterations(oracle):
     assert rel.reshape(net.N, -1)[:, ok].max() < 1e-8
     assert b.iterations[ok].mean() < 0.75 * a.iterations[ok].mean()
     assert b.iterations.max() < 200
+
+
+def _fd_blocks(oracle, net, opt, cells, k, key_v, h_rel=1e-6):
+    """Central finite differences of output `key_v` of the oracle's reaction
+    blocks with respect to the free-ion molalities of cell k."""
+    N = net.N
+    one = cells.subset(np.array([k]), net)
+    base = one.copy()
+    fd = np.zeros((N, N))
+    for j in range(N):
+        vals = []
+        for sgn in (1.0, -1.0):
+            c = base.copy()
+            m = c.pri_molal.copy()
+            h = h_rel * m[j]
+            m[j] += sgn * h
+            c.pri_molal = m
+            vals.append(oracle.reaction_blocks(net.as_struct(), opt, c)[key_v][:, 0])
+        fd[:, j] = (vals[0] - vals[1]) / (2 * h_rel * base.pri_molal[j])
+    return fd
+
+
+def test_reaction_blocks_are_derivatives(oracle):
+    """Global-implicit blocks: d total/dm and d total_sorb/dm are the
+    derivatives of the totals (surface complexation exact only with the exact
+    option); the reaction Jacobian is that of the reaction residual up to
+    RKineticMineral's den/1000 factor (exact with the option)."""
+    net, opt, cells, dt = workloads.synthetic_cells(6, seed=23)
+    sol = cells.copy()
+    oracle.react(net.as_struct(), opt, dt, sol, 0, 2)
+    exact = workloads.default_options(use_isothermal=1, jacobian=abi.JACOBIAN_EXACT)
+    rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()
+    for k in range(cells.ncells):
+        if sol.status[k] != 0:
+            continue
+        one = sol.subset(np.array([k]), net)
+        bx = oracle.reaction_blocks(net.as_struct(), exact, one.copy())
+        br = oracle.reaction_blocks(net.as_struct(), opt, one.copy())
+        # blocks are [cell, j, i]: transpose to [i, j]
+        assert rel(bx["dtotal"][0].T, _fd_blocks(oracle, net, exact, sol, k, "total")) < 1e-6
+        assert rel(bx["dtotal_sorb"][0].T, _fd_blocks(oracle, net, exact, sol, k, "total_sorb")) < 1e-6
+        fd_r = _fd_blocks(oracle, net, exact, sol, k, "res")
+        if np.abs(fd_r).max() > 0:
+            assert rel(bx["jac"][0].T, fd_r) < 1e-5
+        # the reference's aqueous block is exact, its sorbed and reaction blocks are not
+        assert rel(br["dtotal"][0].T, bx["dtotal"][0].T) < 1e-12
+        np.testing.assert_array_equal(br["res"], bx["res"])

@@ -78,3 +78,28 @@ def test_alternative_guess_choice(oracle):
     oracle.react(net.as_struct(), opt, dt, bad, 0, 4)
     assert np.array_equal(bad.pri_molal, plain.pri_molal)
     assert np.array_equal(bad.iterations, plain.iterations)
+
+
+def test_mineral_property_update(oracle):
+    """Porosity = max(1 - sum phi_m, min) and area = area0 (phi/phi0)^p_vf
+    (por/por0)^p_por, with phi0 = 0 keeping the volume-fraction factor at 1."""
+    from pflotran_gb300 import abi, workloads
+    net, opt, cells, dt = workloads.synthetic_cells(64, seed=5)
+    n, Nm = cells.ncells, net.Nm
+    rng = np.random.default_rng(1)
+    cells.mnrl_volfrac = rng.uniform(0.0, 0.05, Nm * n)
+    vf0 = rng.uniform(0.0, 0.05, Nm * n)
+    vf0[::7] = 0.0
+    arrays = {"surf_area_vol_frac_pwr": np.full(Nm, 2.0 / 3.0), "surf_area_porosity_pwr": np.linspace(0.5, 1.5, Nm),
+              "mnrl_volfrac0": vf0, "mnrl_area0": rng.uniform(0.5, 2.0, Nm * n), "porosity0": np.full(n, 0.3),
+              "porosity": np.zeros(n)}
+    mu = abi.mineral_update(arrays, surface_area_with_porosity=1, minimum_porosity=0.75)
+    oracle.update_mineral_properties(net.as_struct(), cells, mu)
+    vf = cells.mnrl_volfrac.reshape(Nm, n)
+    por = np.maximum(1.0 - vf.sum(0), 0.75)
+    assert np.array_equal(arrays["porosity"], por)
+    v0 = vf0.reshape(Nm, n)
+    vs = np.where(v0 > 0, (vf / np.where(v0 > 0, v0, 1.0)) ** (2.0 / 3.0), 1.0)
+    ps = (por / 0.3)[None, :] ** arrays["surf_area_porosity_pwr"][:, None]
+    want = arrays["mnrl_area0"].reshape(Nm, n) * ps * vs
+    np.testing.assert_allclose(cells.mnrl_area.reshape(Nm, n), want, rtol=1e-14)

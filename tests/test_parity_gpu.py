@@ -270,3 +270,60 @@ def test_exact_jacobian(oracle, variant):
     assert errs["total"] <= 1e-9 and errs["mnrl_rate"] <= 1e-9 and errs["mnrl_volfrac"] <= 1e-9, errs
     assert errs["pri_molal"] <= 1e-8, errs
     assert g.iterations[both].mean() < 0.8 * base.iterations[both].mean()
+
+
+@pytest.mark.parametrize("kind,jac", [("synthetic", abi.JACOBIAN_REFERENCE), ("synthetic", abi.JACOBIAN_EXACT),
+                                      ("calcite", abi.JACOBIAN_REFERENCE)])
+def test_reaction_blocks(oracle, kind, jac):
+    """Global-implicit per-cell blocks (residual, Jacobian, totals and their
+    derivatives) against the oracle at the same state; each block compared
+    with its own largest entry as the scale."""
+    if kind == "calcite":
+        net, opt, cells, dt = workloads.calcite_cells(2048, seed=31, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(2048, seed=32)
+    opt.jacobian = jac
+    cells.sec_molal = np.zeros(max(net.Nc, 1) * cells.ncells)
+    ref = cells.copy()
+    d = cells.copy().to_device()
+    bo = oracle.reaction_blocks(net.as_struct(), opt, ref)
+    step = ReactionStep(net, opt)
+    bg = {k: v.cpu().numpy() for k, v in step.reaction_blocks(d).items()}
+    g = d.to_host()
+    ok = (ref.status == 0) & (g.status == 0)
+    assert ok.mean() > 0.99
+    for k in ("jac", "dtotal", "dtotal_sorb"):
+        scale = np.abs(bo[k]).max(axis=(1, 2), keepdims=True) + 1e-300
+        err = (np.abs(bg[k] - bo[k]) / scale)[ok].max()
+        assert err <= 1e-10, (k, err)
+    for k in ("res", "total", "total_sorb"):
+        scale = np.abs(bo[k]).max(axis=0, keepdims=True) + 1e-300
+        err = (np.abs(bg[k] - bo[k]) / scale)[:, ok].max()
+        assert err <= 1e-10, (k, err)
+    rate_scale = np.abs(ref.mnrl_rate).reshape(-1, cells.ncells).max(axis=0) + 1e-300
+    err = (np.abs(g.mnrl_rate - ref.mnrl_rate).reshape(-1, cells.ncells) / rate_scale)[:, ok].max()
+    assert err <= 1e-10
+
+
+def test_mineral_property_update(oracle):
+    """Porosity and mineral surface area from the volume fractions, GPU vs oracle."""
+    import torch
+    net, opt, cells, dt = workloads.synthetic_cells(4096, seed=33)
+    n, Nm = cells.ncells, net.Nm
+    rng = np.random.default_rng(3)
+    cells.mnrl_volfrac = rng.uniform(0.0, 0.05, Nm * n)
+    vf0 = rng.uniform(0.0, 0.05, Nm * n)
+    vf0[::5] = 0.0
+    host = {"surf_area_vol_frac_pwr": np.full(Nm, 2.0 / 3.0), "surf_area_porosity_pwr": np.linspace(0.5, 1.5, Nm),
+            "mnrl_volfrac0": vf0, "mnrl_area0": rng.uniform(0.5, 2.0, Nm * n), "porosity0": np.full(n, 0.3),
+            "porosity": np.zeros(n)}
+    dev = {k: torch.as_tensor(v, device="cuda") for k, v in host.items()}
+    ref = cells.copy()
+    oracle.update_mineral_properties(net.as_struct(), ref,
+                                     abi.mineral_update(host, surface_area_with_porosity=1, minimum_porosity=0.76))
+    step = ReactionStep(net, opt)
+    d = cells.to_device()
+    step.update_mineral_properties(d, abi.mineral_update(dev, surface_area_with_porosity=1, minimum_porosity=0.76))
+    g = d.to_host()
+    np.testing.assert_array_equal(dev["porosity"].cpu().numpy(), host["porosity"])
+    np.testing.assert_allclose(g.mnrl_area, ref.mnrl_area, rtol=1e-14, atol=0)
