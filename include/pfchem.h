@@ -314,6 +314,38 @@ typedef struct pfchem_reaction_blocks_out {
 } pfchem_reaction_blocks_out;
 int pfchem_reaction_blocks(pfchem_ctx *ctx, pfchem_cells *cells, pfchem_reaction_blocks_out *out);
 
+/* Batched constraint speciation (ReactionEquilibrateConstraint,
+ * reaction.F90:1308-2046): the free-ion molalities of waters specified by one
+ * constraint per primary species -- the initial and boundary waters of a
+ * run, and the learned warm start's training waters.  Types (and mineral
+ * ids) are shared by the batch, values are per cell.  Rows: TOTAL [mol/L],
+ * FREE [mol/L], LOG (log10 of a free concentration [mol/L]), CHARGE_BAL
+ * (value: initial guess [mol/L]), PH (the component is H+; value: pH) and
+ * MINERAL (the reaction of kinetic mineral mineral[i] held at equilibrium;
+ * value: initial guess [mol/L]).  Starts from free ions 1e-9, alternates log
+ * and linear updates for iterations 4-8, switches activity coefficients on
+ * after the first convergence; converged when max|res| <
+ * opt.max_residual_tolerance and the relative change <
+ * opt.max_relative_change_tolerance.  Device pointers.  Writes pri_molal,
+ * total_out, sec_molal, total_sorb_eq, the sorption warm starts,
+ * ionic_strength, iterations and status (0 converged, 1 iteration cap,
+ * 2 singular, 3 non-positive molality) of every cell; cells->total is not
+ * read.  Returns the number of cells that did not converge, or < 0. */
+#define PFCHEM_CONSTRAINT_TOTAL 1
+#define PFCHEM_CONSTRAINT_FREE 2
+#define PFCHEM_CONSTRAINT_CHARGE_BAL 3
+#define PFCHEM_CONSTRAINT_PH 4
+#define PFCHEM_CONSTRAINT_LOG 5
+#define PFCHEM_CONSTRAINT_MINERAL 6
+typedef struct pfchem_constraint {
+  const int32_t *type;     /* (naqcomp) PFCHEM_CONSTRAINT_* (host pointer) */
+  const int32_t *mineral;  /* (naqcomp) 1-based kinetic mineral of MINERAL rows, or NULL (host pointer) */
+  const double *value;     /* (naqcomp, ncells) per-cell values (device pointer) */
+  int32_t max_iterations;  /* cap; <= 0 means 10000 */
+  int32_t reserved;
+} pfchem_constraint;
+int pfchem_equilibrate_constraints(pfchem_ctx *ctx, pfchem_cells *cells, const pfchem_constraint *con);
+
 /* Mineral-driven porosity and surface-area update after the kinetic state
  * (RealizationUpdatePropertiesTS, realization_subsurface.F90:1686-1735, and
  * RealizationCalcMineralPorosity, :1946-2001):

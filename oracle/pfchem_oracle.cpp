@@ -1453,17 +1453,19 @@ double pfo_ifc67_density(double t, double p) {
 
 namespace {
 // Constraint row types of ReactionEquilibrateConstraint (reaction_aux.F90 CONSTRAINT_*)
-enum { kConTotal = 1, kConFree = 2, kConChargeBal = 3 };
+enum { kConTotal = 1, kConFree = 2, kConChargeBal = 3, kConPH = 4, kConLog = 5, kConMineral = 6 };
 
-// reaction.F90:1308-2046 ReactionEquilibrateConstraint, restricted to TOTAL,
-// FREE and CHARGE_BAL rows (no minerals/gases/pH rows): the initial-condition
-// speciation of the known-answer decks.  Starts from free ions 1e-9
-// (reaction.F90:1481), alternates log/linear updates for iterations 4-8
-// (:1841-1852) and switches activity coefficients on after the first
-// convergence (:1954-1966).
+// reaction.F90:1308-2046 ReactionEquilibrateConstraint with TOTAL [mol/L],
+// FREE [mol/L], LOG (log10 free [mol/L]), CHARGE_BAL, pH (H+ as a primary
+// species) and MINERAL rows (no gas, sorbed-total or colloid rows); a MINERAL
+// row holds the reaction of kinetic mineral `mineral[i]` (1-based) at
+// equilibrium.  Starts from free ions 1e-9 (reaction.F90:1481), alternates
+// log/linear updates for iterations 4-8 (:1841-1852) and switches activity
+// coefficients on after the first convergence (:1954-1966).  Returns 0,
+// 1 (iteration cap), 2 (singular), 3 (non-positive molality, :1876-1894).
 template <class R>
 int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, const int *type,
-                           const double *conc, int *iters_out) {
+                           const double *conc, int *iters_out, const int *mineral = nullptr, int max_its = 10000) {
   const int N = w.N;
   const pfchem_network &n = *w.n;
   R convert_molar_to_molal = R(1000) / c.den_kg;
@@ -1472,7 +1474,10 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
     free_conc[i] = R(1e-9);
     total_conc[i] = 0;
     if (type[i] == kConTotal) total_conc[i] = R(conc[i]);
-    else if (type[i] == kConFree || type[i] == kConChargeBal) free_conc[i] = R(conc[i]) * convert_molar_to_molal;
+    else if (type[i] == kConFree || type[i] == kConChargeBal || type[i] == kConMineral)
+      free_conc[i] = R(conc[i]) * convert_molar_to_molal;
+    else if (type[i] == kConLog) free_conc[i] = std::pow(R(10), R(conc[i])) * convert_molar_to_molal;
+    else if (type[i] == kConPH) free_conc[i] = std::pow(R(10), -R(conc[i]));
   }
   for (int i = 0; i < N; ++i) c.pri_molal[i] = free_conc[i];
   for (int i = 0; i < N; ++i) c.pri_act_coef[i] = 1;
@@ -1485,7 +1490,7 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
   R Res[P], Jac[P][P], update[P], prev[P];
   for (;;) {
     for (int i = 0; i < N; ++i)
-      if (type[i] == kConFree) c.pri_molal[i] = free_conc[i];
+      if (type[i] == kConFree || type[i] == kConLog) c.pri_molal[i] = free_conc[i];
     if (o.act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF && compute_activity_coefs)
       activity_coefficients(w, o, c, false, R(0));
     rtotal(w, c);
@@ -1495,9 +1500,26 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
       if (type[i] == kConTotal) {
         Res[i] = c.total[i] - total_conc[i];
         for (int j = 0; j < N; ++j) Jac[i][j] = c.dtotal[i][j];
-      } else if (type[i] == kConFree) {
+      } else if (type[i] == kConFree || type[i] == kConLog) {
         Res[i] = 0;
         Jac[i][i] = 1;
+      } else if (type[i] == kConPH) {  // reaction.F90:1653-1661 (H+ primary)
+        Res[i] = 0;
+        c.pri_molal[i] = std::pow(R(10), -R(conc[i])) / c.pri_act_coef[i];
+        Jac[i][i] = 1;
+      } else if (type[i] == kConMineral) {  // reaction.F90:1694-1717
+        const int m = mineral[i] - 1;
+        R lnQK = -c.kinmnrl_logK[m] * R(kLOG_TO_LN);
+        if (n.kinmnrlh2oid && n.kinmnrlh2oid[m] > 0) lnQK = lnQK + R(n.kinmnrlh2ostoich[m]) * c.ln_act_h2o;
+        for (int k = 1; k <= w.mn(m); ++k) {
+          const int j = w.mid(m, k);
+          lnQK = lnQK + R(w.mnu(m, k)) * rlog(c.pri_molal[j] * c.pri_act_coef[j]);
+        }
+        Res[i] = lnQK;
+        for (int k = 1; k <= w.mn(m); ++k) {
+          const int j = w.mid(m, k);
+          Jac[i][j] = R(w.mnu(m, k)) / c.pri_molal[j];
+        }
       } else {  // charge balance (reaction.F90:1623-1634)
         Res[i] = 0;
         for (int j = 0; j < N; ++j) {
@@ -1534,10 +1556,12 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
         for (int i = 0; i < N; ++i) update[i] = update[i] * min_ratio * R(0.99);
       for (int i = 0; i < N; ++i) c.pri_molal[i] = prev[i] - update[i];
     }
+    for (int i = 0; i < N; ++i)
+      if (!(c.pri_molal[i] > 0)) return 3;
     R mrc = 0;
     for (int i = 0; i < N; ++i) mrc = std::max(mrc, std::fabs((c.pri_molal[i] - prev[i]) / prev[i]));
     ++num_iterations;
-    if (num_iterations >= 10000) return 1;
+    if (num_iterations >= max_its) return 1;
     if (maximum_residual < R(o.max_residual_tolerance) && mrc < R(o.max_relative_change_tolerance)) {
       if (compute_activity_coefs && num_iterations - num_it_act_coef_turned_on > 1) break;
       if (!compute_activity_coefs) num_it_act_coef_turned_on = num_iterations;
@@ -1559,6 +1583,52 @@ extern "C" {
 // type[i]: 1 TOTAL [mol/L], 2 FREE [mol/L], 3 CHARGE_BAL (conc = guess).
 // Writes pri_molal, total_out, sec_molal, sorption state and the ionic
 // strength (at the final state, recomputed as the next LAG update would).
+// Constraint speciation of every cell of `cells` (host pointers): one
+// constraint row per component (types and mineral ids shared by the batch,
+// values per cell), `nthreads` std::threads.  Writes what the single-cell
+// entry below writes, plus iterations and status (0 converged, 1 cap,
+// 2 singular, 3 non-positive molality).  Returns the number of failed cells.
+int pfo_equilibrate_constraints(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
+                                const pfchem_constraint *con, int nthreads) {
+  Net w = make_net(net, opt);
+  const int64_t n = cells->ncells;
+  std::atomic<int> bad{0};
+  auto work = [&](int64_t k0, int64_t k1) {
+    for (int64_t k = k0; k < k1; ++k) {
+      Cell<double> c;
+      load_cell(w, cells, k, c);
+      update_temp_dependent_coefs(w, *opt, c);
+      double conc[P];
+      for (int j = 0; j < w.N; ++j) conc[j] = con->value[j * n + k];
+      int its = 0;
+      const int r = equilibrate_constraint(w, *opt, c, con->type, conc, &its, con->mineral,
+                                           con->max_iterations > 0 ? con->max_iterations : 10000);
+      if (r) bad++;
+      for (int j = 0; j < w.N; ++j) {
+        cells->pri_molal[j * n + k] = c.pri_molal[j];
+        if (cells->total_out) cells->total_out[j * n + k] = c.total[j];
+        if (cells->total_sorb_eq) cells->total_sorb_eq[j * n + k] = c.total_sorb_eq[j];
+      }
+      for (int i = 0; i < w.Nc; ++i)
+        if (cells->sec_molal) cells->sec_molal[i * n + k] = c.sec_molal[i];
+      for (int q = 0; q < w.Nix; ++q) cells->eqionx_ref_cation_sorbed_conc[q * n + k] = c.eqionx_ref_cation_sorbed_conc[q];
+      for (int q = 0; q < w.Nsr; ++q) cells->srfcplxrxn_free_site_conc[q * n + k] = c.srfcplxrxn_free_site_conc[q];
+      cells->ionic_strength[k] = ionic_strength_of(w, c);
+      if (cells->iterations) cells->iterations[k] = its;
+      if (cells->status) cells->status[k] = r;
+    }
+  };
+  if (nthreads < 1) nthreads = 1;
+  std::vector<std::thread> pool;
+  const int64_t chunk = (n + nthreads - 1) / nthreads;
+  for (int t = 0; t < nthreads; ++t) {
+    const int64_t k0 = t * chunk, k1 = std::min(n, k0 + chunk);
+    if (k0 < k1) pool.emplace_back(work, k0, k1);
+  }
+  for (auto &th : pool) th.join();
+  return bad.load();
+}
+
 int pfo_equilibrate_constraint(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
                                const int *type, const double *conc, int *iters) {
   Net w = make_net(net, opt);

@@ -23,6 +23,8 @@ namespace pfchem {
 cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
                          cudaStream_t st);
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
+cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const int32_t *type, const int32_t *mineral,
+                              const double *value, int max_its, Scratch *scr, cudaStream_t st);
 cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, cudaStream_t st);
 cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
                                    double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st);
@@ -711,6 +713,38 @@ int pfchem_reaction_blocks(pfchem_ctx *c, pfchem_cells *cl, pfchem_reaction_bloc
   if (le != cudaSuccess) return fail(c, -2, "reaction-blocks launch: %s", cudaGetErrorString(le));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return 0;
+}
+
+int pfchem_equilibrate_constraints(pfchem_ctx *c, pfchem_cells *cl, const pfchem_constraint *con) {
+  if (!c || !cl || !con || !con->type || !con->value) return fail(c, -1, "null argument");
+  if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
+  if (!cl->on_device) return fail(c, -1, "pfchem_equilibrate_constraints takes device pointers");
+  const DevNet &n = c->net;
+  if (!cl->temperature || !cl->den_kg || !cl->pri_molal || !cl->ionic_strength || !cl->porosity || !cl->saturation ||
+      !cl->volume)
+    return fail(c, -1, "a required per-cell array is null");
+  if (n.Nm > 0 && (!cl->mnrl_volfrac || !cl->mnrl_area)) return fail(c, -1, "mnrl_volfrac/mnrl_area required");
+  if (n.Nix + n.Nsr > 0 && (!cl->total_sorb_eq || (n.Nix && !cl->eqionx_ref_cation_sorbed_conc) ||
+                            (n.Nsr && !cl->srfcplxrxn_free_site_conc)))
+    return fail(c, -1, "sorption state arrays required");
+  for (int j = 0; j < n.N; ++j) {
+    const int t = con->type[j];
+    if (t < PFCHEM_CONSTRAINT_TOTAL || t > PFCHEM_CONSTRAINT_MINERAL)
+      return fail(c, -1, "component %d: unknown constraint type %d", j + 1, t);
+    if (t == PFCHEM_CONSTRAINT_MINERAL && (!con->mineral || con->mineral[j] < 1 || con->mineral[j] > n.Nm))
+      return fail(c, -1, "component %d: MINERAL row needs a kinetic mineral id in [1,%d]", j + 1, n.Nm);
+  }
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  CUDA_TRY(c, cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream));
+  cudaError_t le = launch_constraint(n, a, con->type, con->mineral, con->value,
+                                     con->max_iterations > 0 ? con->max_iterations : 10000, c->scratch, c->stream);
+  if (le != cudaSuccess) return fail(c, -2, "constraint launch: %s", cudaGetErrorString(le));
+  Scratch h;
+  CUDA_TRY(c, cudaMemcpyAsync(&h, c->scratch, sizeof(Scratch), cudaMemcpyDeviceToHost, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return (int)h.nonconverged;
 }
 
 int pfchem_update_mineral_properties(pfchem_ctx *c, pfchem_cells *cl, const pfchem_mineral_update *mu) {

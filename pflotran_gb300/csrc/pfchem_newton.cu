@@ -938,6 +938,214 @@ static cudaError_t launch_blocks_t(const DevNet &n, const CellArgs &a, const Blo
   return cudaGetLastError();
 }
 
+// Batched constraint speciation (ReactionEquilibrateConstraint,
+// reaction.F90:1308-2046), one thread per cell: Newton on the constraint
+// rows with the aqueous totals and their derivatives from the same
+// evaluation the reaction step uses (accumulation and mineral weights zero,
+// d total/d ln m in the shared-memory system).
+struct ConstraintRows {
+  int8_t type[PFCHEM_MAX_PRI];
+  int8_t mineral[PFCHEM_MAX_PRI];  // 0-based kinetic mineral of MINERAL rows
+  int32_t max_its;
+  const double *value;             // (N, ncells)
+};
+
+template <class S>
+__global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ DevNet n,
+                                                        const __grid_constant__ CellArgs a,
+                                                        const __grid_constant__ ConstraintRows con, Scratch *scr) {
+  extern __shared__ double smem[];
+  const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (cell >= a.ncells) return;
+  const int N = n.N;
+  const int64_t nc = a.ncells;
+  double *J = smem + threadIdx.x;
+  const int js = blockDim.x;
+  Lane<S> L;
+  setup(n, a, cell, L, 1.0);
+  // activity coefficients start at 1 (reaction.F90:1308-1478)
+  for (int j = 0; j < N; ++j) {
+    L.lngp[j] = 0.0;
+    L.gp[j] = 1.0;
+  }
+  for (int i = 0; i < n.Nc; ++i) L.bc[i] = L.bK[i];
+  L.acc = 0.0;
+  for (int j = 0; j < N; ++j) L.fixed[j] = L.absfixed[j] = 0.0;
+  L.jac_aq = L.den_L;  // d(total [mol/L]) / d ln m
+  L.v_t = 0.0;
+  L.jac_mnrl = 0.0;
+  const double molar_to_molal = 1000.0 / a.den[cell];
+  double freec[S::NP], totc[S::NP], val[S::NP], res[S::NP], prev[S::NP];
+  for (int j = 0; j < N; ++j) {
+    val[j] = con.value[j * nc + cell];
+    freec[j] = 1e-9;
+    totc[j] = 0.0;
+    switch (con.type[j]) {
+      case PFCHEM_CONSTRAINT_TOTAL: totc[j] = val[j]; break;
+      case PFCHEM_CONSTRAINT_FREE:
+      case PFCHEM_CONSTRAINT_CHARGE_BAL:
+      case PFCHEM_CONSTRAINT_MINERAL: freec[j] = val[j] * molar_to_molal; break;
+      case PFCHEM_CONSTRAINT_LOG: freec[j] = pow(10.0, val[j]) * molar_to_molal; break;
+      case PFCHEM_CONSTRAINT_PH: freec[j] = pow(10.0, -val[j]); break;
+      default: break;
+    }
+    L.m[j] = freec[j];
+  }
+  bool act = false;
+  int its = 0, its_on = 0, status = 1;
+  for (;;) {
+    for (int j = 0; j < N; ++j) {
+      if (con.type[j] == PFCHEM_CONSTRAINT_FREE || con.type[j] == PFCHEM_CONSTRAINT_LOG) L.m[j] = freec[j];
+      L.lnm[j] = log(L.m[j]);
+    }
+    if (act && n.act_freq != PFCHEM_ACT_COEF_FREQUENCY_OFF) {
+      // ionic strength of the current free ions and the last complexes
+      double I = 0.0;
+      for (int j = 0; j < N; ++j) I += n.Z2p[j] * L.m[j];
+      for (int i = 0; i < n.Nc; ++i) I += n.cZ2[i] * L.C[i];
+      activity(n, L, 0.5 * I);
+    }
+    if (evaluate<S, true>(n, L, J, js)) {
+      status = 1;
+      break;
+    }
+    // rows in d/dm, as ReactionEquilibrateConstraint forms them (reaction.F90:1597-1717)
+    for (int k = 0; k < N; ++k) {
+      const double im = 1.0 / L.m[k];
+      for (int i = 0; i < N; ++i) J[(i * N + k) * js] *= im;
+    }
+    double cb[S::NP];
+    bool any_cb = false;
+    for (int j = 0; j < N; ++j) any_cb |= con.type[j] == PFCHEM_CONSTRAINT_CHARGE_BAL;
+    if (any_cb)
+      for (int k = 0; k < N; ++k) {
+        double s = 0.0;
+        for (int i = 0; i < N; ++i) s += n.Zp[i] * J[(i * N + k) * js];
+        cb[k] = s;
+      }
+    double maxres = 0.0;
+    for (int i = 0; i < N; ++i) {
+      switch (con.type[i]) {
+        case PFCHEM_CONSTRAINT_TOTAL: res[i] = L.Psi[i] * L.den_L - totc[i]; break;
+        case PFCHEM_CONSTRAINT_CHARGE_BAL: {
+          double s = 0.0;
+          for (int j = 0; j < N; ++j) s += n.Zp[j] * (L.Psi[j] * L.den_L);
+          res[i] = s;
+          for (int k = 0; k < N; ++k) J[(i * N + k) * js] = cb[k];
+          break;
+        }
+        case PFCHEM_CONSTRAINT_MINERAL: {
+          const int mm = con.mineral[i];
+          double lnQK = L.bm[mm];
+          for (int k = 0; k < n.mn[mm]; ++k) {
+            const int j = n.mid[mm][k];
+            lnQK += n.mnu[mm][k] * log(L.m[j] * L.gp[j]);
+          }
+          res[i] = lnQK;
+          for (int k = 0; k < N; ++k) J[(i * N + k) * js] = 0.0;
+          for (int k = 0; k < n.mn[mm]; ++k) {
+            const int j = n.mid[mm][k];
+            J[(i * N + j) * js] = n.mnu[mm][k] / L.m[j];
+          }
+          break;
+        }
+        default: {  // FREE, LOG, PH: identity row
+          if (con.type[i] == PFCHEM_CONSTRAINT_PH) L.m[i] = pow(10.0, -val[i]) / L.gp[i];
+          res[i] = 0.0;
+          for (int k = 0; k < N; ++k) J[(i * N + k) * js] = (k == i) ? 1.0 : 0.0;
+          break;
+        }
+      }
+      maxres = fmax(maxres, fabs(res[i]));
+    }
+    bool use_log = false;
+    if (n.use_log) use_log = (its > 3 && its < 9) ? (its % 2 == 0) : true;
+    if (use_log)  // RSolve's log form scales the columns by the molalities
+      for (int k = 0; k < N; ++k)
+        for (int i = 0; i < N; ++i) J[(i * N + k) * js] *= L.m[k];
+    if (!lu_solve(J, js, N, res)) {
+      status = 2;
+      break;
+    }
+    bool nonpos = false;
+    double mrc = 0.0;
+    if (use_log) {
+      for (int j = 0; j < N; ++j) {
+        prev[j] = L.m[j];
+        const double u = copysign(fmin(fabs(res[j]), n.max_dlnC), res[j]);
+        L.m[j] = L.m[j] * exp(-u);
+      }
+    } else {
+      double min_ratio = 1e20;
+      for (int j = 0; j < N; ++j) {
+        prev[j] = L.m[j];
+        if (prev[j] <= res[j]) {
+          const double ratio = fabs(prev[j] / res[j]);
+          if (ratio < min_ratio) min_ratio = ratio;
+        }
+      }
+      const double sc = (min_ratio <= 1.0) ? min_ratio * 0.99 : 1.0;
+      for (int j = 0; j < N; ++j) L.m[j] = prev[j] - (min_ratio <= 1.0 ? res[j] * sc : res[j]);
+    }
+    for (int j = 0; j < N; ++j) {
+      if (!(L.m[j] > 0.0)) nonpos = true;
+      mrc = fmax(mrc, fabs((L.m[j] - prev[j]) / prev[j]));
+    }
+    if (nonpos) {
+      status = 3;
+      break;
+    }
+    ++its;
+    if (its >= con.max_its) {
+      status = 1;
+      break;
+    }
+    if (maxres < n.res_tol && mrc < n.rel_change_tol) {
+      if (act && its - its_on > 1) {
+        status = 0;
+        break;
+      }
+      if (!act) its_on = its;
+      act = true;
+    }
+  }
+  // totals and sorption at the final free ions with the last activity
+  // coefficients (what the next step's RTAuxVarCompute sees)
+  for (int j = 0; j < N; ++j) L.lnm[j] = log(L.m[j]);
+  if (status == 0 && evaluate<S, true>(n, L, J, js)) status = 1;
+  double I = 0.0;
+  for (int j = 0; j < N; ++j) {
+    a.pri_molal[j * nc + cell] = L.m[j];
+    if (a.total_out) a.total_out[j * nc + cell] = L.Psi[j] * L.den_L;
+    if (a.sorb) a.sorb[j * nc + cell] = L.S_[j];
+    I += n.Z2p[j] * L.m[j];
+  }
+  for (int i = 0; i < n.Nc; ++i) {
+    if (a.sec_molal) a.sec_molal[i * nc + cell] = L.C[i];
+    I += n.cZ2[i] * L.C[i];
+  }
+  a.ionic[cell] = 0.5 * I;
+  for (int r = 0; r < n.Nix; ++r) a.ixref[r * nc + cell] = L.ixref[r];
+  for (int r = 0; r < n.Nsr; ++r) a.srfree[r * nc + cell] = L.srfree[r];
+  if (a.iters) a.iters[cell] = its;
+  if (a.status) a.status[cell] = status;
+  if (status != 0) atomicAdd(&scr->nonconverged, 1u);
+}
+
+template <class S>
+static cudaError_t launch_constraint_t(const DevNet &n, const CellArgs &a, const ConstraintRows &c, Scratch *scr,
+                                       cudaStream_t st) {
+  const int block = 32;
+  const size_t shm = (size_t)n.N * n.N * block * sizeof(double);
+  if (shm > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(constraint_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm);
+    if (e != cudaSuccess) return e;
+  }
+  const int64_t grid = (a.ncells + block - 1) / block;
+  constraint_kernel<S><<<(unsigned)grid, block, shm, st>>>(n, a, c, scr);
+  return cudaGetLastError();
+}
+
 // Mineral-driven porosity and surface area (one thread per cell).
 __global__ void __launch_bounds__(128) mineral_properties_kernel(const __grid_constant__ CellArgs a, int Nm,
                                                                  pfchem_mineral_update mu) {
@@ -1016,6 +1224,22 @@ cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *r
     case 0: return launch_blocks_t<SizesS>(n, a, o, st);
     case 1: return launch_blocks_t<SizesM>(n, a, o, st);
     default: return launch_blocks_t<SizesL>(n, a, o, st);
+  }
+}
+
+cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const int32_t *type, const int32_t *mineral,
+                              const double *value, int max_its, Scratch *scr, cudaStream_t st) {
+  ConstraintRows c{};
+  for (int j = 0; j < n.N; ++j) {
+    c.type[j] = (int8_t)type[j];
+    c.mineral[j] = (int8_t)(mineral && mineral[j] > 0 ? mineral[j] - 1 : 0);
+  }
+  c.max_its = max_its;
+  c.value = value;
+  switch (size_class(n)) {
+    case 0: return launch_constraint_t<SizesS>(n, a, c, scr, st);
+    case 1: return launch_constraint_t<SizesM>(n, a, c, scr, st);
+    default: return launch_constraint_t<SizesL>(n, a, c, scr, st);
   }
 }
 
