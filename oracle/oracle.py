@@ -37,6 +37,7 @@ def lib():
         l.pfo_interpolate_logK.argtypes = [C.c_void_p, C.c_double]
         l.pfo_interpolate_logK.restype = C.c_double
         l.pfo_ifc67_density.argtypes = [C.c_double, C.c_double]
+        l.pfo_equilibrate_constraints.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]
         l.pfo_update_mineral_properties.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         l.pfo_reaction_blocks.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         l.pfo_newton_system.argtypes = [C.c_void_p, C.c_void_p, C.c_double, C.c_void_p, C.c_int64, C.c_void_p,
@@ -137,3 +138,17 @@ def update_mineral_properties(net_struct, cells, mu):
     """Restated porosity / mineral surface-area update on a host CellBatch."""
     s = cells.struct()
     return lib().pfo_update_mineral_properties(C.byref(net_struct), C.byref(s), C.byref(mu))
+
+
+def equilibrate_constraints(net_struct, opt, cells, types, values, minerals=None, max_iterations=0, nthreads=None):
+    """Restated constraint speciation of every cell of a host CellBatch;
+    `values` (N, ncells).  Returns the number of failed cells."""
+    from pflotran_gb300 import abi
+    t = np.ascontiguousarray(types, np.int32)
+    mn = None if minerals is None else np.ascontiguousarray(minerals, np.int32)
+    v = np.ascontiguousarray(values, np.float64)
+    con = abi.Constraint(t.ctypes.data, None if mn is None else mn.ctypes.data, v.ctypes.data,
+                         int(max_iterations), 0)
+    s = cells.struct()
+    return lib().pfo_equilibrate_constraints(C.byref(net_struct), C.byref(opt), C.byref(s), C.byref(con),
+                                             nthreads or os.cpu_count() or 1)

@@ -156,3 +156,11 @@ def mineral_update(arrays, update_porosity=1, update_surface_area=1, surface_are
     return MineralUpdate(update_porosity, update_surface_area, surface_area_with_porosity, 0, minimum_porosity,
                          ptr("surf_area_vol_frac_pwr"), ptr("surf_area_porosity_pwr"), ptr("mnrl_volfrac0"),
                          ptr("mnrl_area0"), ptr("porosity0"), ptr("porosity"))
+
+CONSTRAINT_TOTAL, CONSTRAINT_FREE, CONSTRAINT_CHARGE_BAL, CONSTRAINT_PH, CONSTRAINT_LOG, CONSTRAINT_MINERAL = 1, 2, 3, 4, 5, 6
+
+
+class Constraint(C.Structure):
+    """pfchem_constraint."""
+    _fields_ = [("type", C.c_void_p), ("mineral", C.c_void_p), ("value", C.c_void_p),
+                ("max_iterations", C.c_int32), ("reserved", C.c_int32)]

@@ -65,6 +65,7 @@ def load(build_if_missing=True):
     l.pfchem_autotune.argtypes = [vp, C.c_double, C.POINTER(abi.Cells)]
     l.pfchem_reaction_blocks.argtypes = [vp, C.POINTER(abi.Cells), C.POINTER(abi.ReactionBlocksOut)]
     l.pfchem_update_mineral_properties.argtypes = [vp, C.POINTER(abi.Cells), C.POINTER(abi.MineralUpdate)]
+    l.pfchem_equilibrate_constraints.argtypes = [vp, C.POINTER(abi.Cells), C.POINTER(abi.Constraint)]
     l.pfchem_reserve.argtypes = [vp, C.c_int64]
     l.pfchem_react_batch_async.argtypes = [vp, C.c_double, C.POINTER(abi.Cells), vp]
     l.pfchem_async_stats.argtypes = [vp, C.POINTER(abi.Stats)]
@@ -249,6 +250,19 @@ class ReactionStep(WarmStartMixin):
         st = abi.Stats()
         self._check(self._lib.pfchem_async_stats(self._ctx, C.byref(st)), "pfchem_async_stats")
         return st
+
+    def equilibrate_constraints(self, cells, types, values, minerals=None, max_iterations=0):
+        """Constraint speciation of every cell of a device batch: `types`
+        (and 1-based `minerals`) per component, `values` a device tensor
+        (N, ncells).  Returns the number of cells that did not converge."""
+        import numpy as np
+        t = np.ascontiguousarray(types, np.int32)
+        mn = None if minerals is None else np.ascontiguousarray(minerals, np.int32)
+        con = abi.Constraint(t.ctypes.data, None if mn is None else mn.ctypes.data, values.data_ptr(),
+                             int(max_iterations), 0)
+        s = cells.struct()
+        return self._check(self._lib.pfchem_equilibrate_constraints(self._ctx, C.byref(s), C.byref(con)),
+                           "pfchem_equilibrate_constraints")
 
     def reaction_blocks(self, cells):
         """Global-implicit per-cell blocks at the cells' current state (device

@@ -51,3 +51,30 @@ def compare(net, gpu, ref, tol=1e-10, mask=None):
         out["sec_molal"] = rel_err(gpu.sec_molal.reshape(-1, n)[:net.Nc], ref.sec_molal.reshape(-1, n)[:net.Nc],
                                    1e-280)[:, mask].max()
     return out
+
+
+def constraint_problem(oracle, net, opt, cells, rows):
+    """Constraint rows and per-cell values that describe each cell's own
+    equilibrium state: rows maps component -> kind ('total', 'ph', 'log',
+    'free', 'mineral:<k>', 'charge'); unspecified components are 'total'.
+    Returns (types, minerals, values[N, ncells])."""
+    n, N = cells.ncells, net.N
+    blocks = oracle.reaction_blocks(net.as_struct(), opt, cells.copy())
+    m = cells.pri_molal.reshape(N, n)
+    molar = m * (cells.den_kg * 1e-3)[None, :]
+    types = np.full(N, abi.CONSTRAINT_TOTAL, np.int32)
+    minerals = np.zeros(N, np.int32)
+    values = blocks["total"].copy()
+    for j, kind in rows.items():
+        if kind == "ph":
+            gp = np.array([oracle.activity_lag(net.as_struct(), float(I), N, net.Nc)[0][j] for I in cells.ionic_strength])
+            types[j], values[j] = abi.CONSTRAINT_PH, -np.log10(m[j] * gp)
+        elif kind == "log":
+            types[j], values[j] = abi.CONSTRAINT_LOG, np.log10(molar[j])
+        elif kind == "free":
+            types[j], values[j] = abi.CONSTRAINT_FREE, molar[j]
+        elif kind == "charge":
+            types[j], values[j] = abi.CONSTRAINT_CHARGE_BAL, molar[j]
+        elif kind.startswith("mineral:"):
+            types[j], minerals[j], values[j] = abi.CONSTRAINT_MINERAL, int(kind.split(":")[1]), molar[j]
+    return types, minerals, np.ascontiguousarray(values)

@@ -1,0 +1,74 @@
+"""PFLOTRAN's own known answers through the GPU path: constraint speciation
+and reaction steps on the device (fixtures from tests/golden/, tolerances
+of the regression harness, regression_tests/ascem/batch/batch.cfg:15-19)."""
+import math
+
+import numpy as np
+import pytest
+
+import kat
+from pflotran_gb300 import abi
+from pflotran_gb300.lib import ReactionStep
+from pflotran_gb300.network import default_options
+
+pytestmark = pytest.mark.gpu
+
+
+def _constraint_on_gpu(net, copt, b, fx, ncopies=64):
+    """The deck's constraint solved for `ncopies` identical cells on the GPU."""
+    import torch
+    from pflotran_gb300.cells import CellBatch
+    idx = np.zeros(ncopies, np.int64)
+    many = b.subset(idx, net)
+    many.iterations = np.zeros(ncopies, np.int32)
+    many.status = np.zeros(ncopies, np.int32)
+    many.total_out = np.zeros(net.N * ncopies)
+    d = many.to_device()
+    step = ReactionStep(net, copt)
+    conc = np.repeat(np.asarray(fx["constraint"]["conc"], np.float64)[:, None], ncopies, axis=1)
+    bad = step.equilibrate_constraints(d, fx["constraint"]["types"], torch.as_tensor(conc, device="cuda"))
+    assert bad == 0
+    return d.to_host()
+
+
+def test_ion_exchange_valocchi_gold_gpu(oracle):
+    fx = kat.load("kat_ion_exchange_valocchi.json")
+    net = kat.build_network(fx, oracle)
+    copt = default_options(use_isothermal=1, act_coef_update_frequency=abi.ACT_COEF_FREQUENCY_OFF,
+                           residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    g = _constraint_on_gpu(net, copt, kat.one_cell(net, fx, oracle), fx)
+    names = [p["name"] for p in fx["primaries"]]
+    n = g.ncells
+    for i, nm in enumerate(names):
+        for key, arr in ((f"Total {nm}", g.total_out), (f"Total Sorbed {nm}", g.total_sorb_eq)):
+            v = arr.reshape(net.N, n)[i]
+            assert np.abs(v - fx["gold"][key]).max() <= 1e-12, (key, v[0], fx["gold"][key])
+
+
+def test_calcite_kinetics_gold_gpu(oracle):
+    """Constraint speciation and 500 reaction steps of 0.5 s on the GPU."""
+    fx = kat.load("kat_calcite_kinetics.json")
+    net = kat.build_network(fx, oracle)
+    copt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    g = _constraint_on_gpu(net, copt, kat.one_cell(net, fx, oracle), fx, ncopies=32)
+    d = g.to_device()
+    sopt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_RELATIVE, max_residual_tolerance=1e-15,
+                           max_relative_change_tolerance=0.0, max_iterations=100, update_kinetic_state=1)
+    step = ReactionStep(net, sopt)
+    I_prev = None
+    for _ in range(fx["nsteps"]):
+        d.total.copy_(d.total_out)
+        I_prev = float(d.ionic_strength[0])
+        assert step.react(d, fx["dt"]) == 0
+    h = d.to_host()
+    gp, _ = oracle.activity_lag(net.as_struct(), I_prev, net.N, net.Nc)
+    n = h.ncells
+    out = {"Total H+": h.total_out.reshape(net.N, n)[0], "Total HCO3-": h.total_out.reshape(net.N, n)[1],
+           "Total Ca++": h.total_out.reshape(net.N, n)[2], "Calcite VF": h.mnrl_volfrac.reshape(-1, n)[0],
+           "Calcite Rate": h.mnrl_rate.reshape(-1, n)[0]}
+    for key, v in out.items():
+        assert np.abs(v - fx["gold"][key]).max() <= 1e-12, (key, v[0], fx["gold"][key])
+    ph = -math.log10(h.pri_molal[0] * gp[0])
+    assert abs(ph - fx["gold"]["pH"]) <= 5e-8

@@ -103,3 +103,33 @@ def test_mineral_property_update(oracle):
     ps = (por / 0.3)[None, :] ** arrays["surf_area_porosity_pwr"][:, None]
     want = arrays["mnrl_area0"].reshape(Nm, n) * ps * vs
     np.testing.assert_allclose(cells.mnrl_area.reshape(Nm, n), want, rtol=1e-14)
+
+
+def test_constraint_rows_are_satisfied(oracle):
+    """Batched constraint speciation with pH, log-free, mineral and total rows:
+    the solution meets every row (pH of the final activity, saturation of the
+    constraining mineral, totals)."""
+    from pflotran_gb300 import abi, workloads
+    from helpers import constraint_problem
+    net, _, cells, dt = workloads.synthetic_cells(64, seed=41)
+    copt = workloads.default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                                     max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    rows = {0: "ph", 5: "log", 3: "mineral:4"}
+    types, minerals, values = constraint_problem(oracle, net, copt, cells, rows)
+    out = cells.copy()
+    out.sec_molal = np.zeros(net.Nc * cells.ncells)
+    bad = oracle.equilibrate_constraints(net.as_struct(), copt, out, types, values, minerals)
+    assert bad == 0, np.bincount(out.status)
+    N, n = net.N, cells.ncells
+    m = out.pri_molal.reshape(N, n)
+    tot = out.total_out.reshape(N, n)
+    for j in range(N):
+        if types[j] == abi.CONSTRAINT_TOTAL:
+            assert np.abs(tot[j] - values[j]).max() <= 1e-10 * np.abs(values[j]).max()
+    np.testing.assert_allclose(np.log10(m[5] * cells.den_kg * 1e-3), values[5], rtol=0, atol=1e-12)
+    # mineral 4 (P2 + P3) at saturation with the final activity coefficients
+    gp = np.array([oracle.activity_lag(net.as_struct(), float(I), N, net.Nc)[0] for I in out.ionic_strength]).T
+    mn = net.minerals[3]
+    lnQK = -mn.logK * 2.30258509299 + sum(nu * np.log(m[net.idx(s)] * gp[net.idx(s)])
+                                         for s, nu in zip(mn.species, mn.stoich))
+    assert np.abs(lnQK).max() < 1e-6

@@ -327,3 +327,28 @@ def test_mineral_property_update(oracle):
     g = d.to_host()
     np.testing.assert_array_equal(dev["porosity"].cpu().numpy(), host["porosity"])
     np.testing.assert_allclose(g.mnrl_area, ref.mnrl_area, rtol=1e-14, atol=0)
+
+
+def test_constraint_speciation(oracle):
+    """Batched constraint speciation (pH, log-free, mineral and total rows),
+    GPU vs oracle on identical inputs."""
+    import torch
+    from helpers import constraint_problem
+    net, _, cells, dt = workloads.synthetic_cells(4096, seed=42)
+    copt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    types, minerals, values = constraint_problem(oracle, net, copt, cells, {0: "ph", 5: "log", 3: "mineral:4"})
+    ref = cells.copy()
+    ref.sec_molal = np.zeros(net.Nc * cells.ncells)
+    d = ref.copy().to_device()
+    bad_ref = oracle.equilibrate_constraints(net.as_struct(), copt, ref, types, values, minerals)
+    step = ReactionStep(net, copt)
+    bad = step.equilibrate_constraints(d, types, torch.as_tensor(values, device="cuda"), minerals)
+    g = d.to_host()
+    # a few cells of this draw cannot reach saturation of the constraining
+    # mineral with the other rows held (the reference's iteration fails too)
+    assert bad <= 0.01 * cells.ncells and bad_ref <= 0.01 * cells.ncells
+    ok = (g.status == 0) & (ref.status == 0)
+    assert ok.sum() >= cells.ncells - max(bad, bad_ref) - 2
+    assert np.mean(g.iterations[ok] == ref.iterations[ok]) > 0.98
+    assert_parity(net, g, ref, mask=ok)
