@@ -426,6 +426,10 @@ int pfchem_surrogate_fit(pfchem_ctx *ctx, const float *X, const double *molal, i
 /* The network's prediction for each cell of `cells` (device) into guess
  * (SoA [naqcomp][ncells] free-ion molalities, device). */
 int pfchem_surrogate_predict(pfchem_ctx *ctx, pfchem_cells *cells, double *guess);
+/* The same prediction through the layer-by-layer path (one GEMM launch per
+ * layer, activations through HBM) that training uses; the warm start itself
+ * runs the fused one-kernel inference.  Kept to check one against the other. */
+int pfchem_surrogate_predict_layers(pfchem_ctx *ctx, pfchem_cells *cells, double *guess);
 /* 1 = predict the alternative guess inside pfchem_react_batch (needs a fit). */
 int pfchem_surrogate_enable(pfchem_ctx *ctx, int on);
 /* Loss and gradients of the current weights on M samples, without updating

@@ -51,6 +51,8 @@ cudaError_t surrogate_set_params(Surrogate *s, const float *host);
 cudaError_t surrogate_prepare(Surrogate *s, long long ncells);
 double *surrogate_guess_buffer(Surrogate *s);
 cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st);
+cudaError_t surrogate_predict_layers(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess,
+                                     cudaStream_t st);
 cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, float *T, cudaStream_t st);
 void surrogate_mark_trained(Surrogate *s, bool t);
 bool surrogate_trained(const Surrogate *s);
@@ -1018,6 +1020,20 @@ int pfchem_surrogate_predict(pfchem_ctx *c, pfchem_cells *cl, double *guess) {
   CUDA_TRY(c, surrogate_predict(c->sur, c->net, a, c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(guess, surrogate_guess_buffer(c->sur), (size_t)c->net.N * a.ncells * sizeof(double),
                               cudaMemcpyDeviceToDevice, c->stream));
+  CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  return 0;
+}
+
+int pfchem_surrogate_predict_layers(pfchem_ctx *c, pfchem_cells *cl, double *guess) {
+  int e = check_cells(c, cl);
+  if (e) return e;
+  if (!cl->on_device || !guess) return fail(c, -1, "device pointers required");
+  if (!c->sur || !surrogate_trained(c->sur)) return fail(c, -1, "the surrogate has not been trained");
+  cudaSetDevice(c->device);
+  CellArgs a = device_args(cl, 1.0);
+  if (a.ncells == 0) return 0;
+  CUDA_TRY(c, surrogate_prepare(c->sur, a.ncells));
+  CUDA_TRY(c, surrogate_predict_layers(c->sur, c->net, a, guess, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
   return 0;
 }

@@ -199,14 +199,11 @@ __global__ void to_bf16(const float *x, bf16 *y, long long n) {
   if (i < n) y[i] = __float2bfloat16(x[i]);
 }
 
-// Per-cell features (raw, before standardisation), row-major [cell][kFeat].
-__global__ void cell_features(const CellArgs a, int N, int sorb, float *X) {
-  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (cell >= a.ncells) return;
+// Per-cell features (raw, before standardisation) of one cell into x[kFeat].
+__device__ __forceinline__ void features_of(const CellArgs &a, int N, int sorb, long long cell, float *x) {
   const long long nc = a.ncells;
   const double por = a.por[cell], sat = a.sat[cell], vol = a.vol[cell];
   const double psv = por * sat * 1000.0 * vol;
-  float *x = X + cell * kFeat;
   for (int j = 0; j < kFeat; ++j) x[j] = 0.f;
   for (int j = 0; j < N; ++j) {
     double acc = psv * a.total[j * a.total_stride_comp + cell * a.total_stride_cell];
@@ -216,6 +213,158 @@ __global__ void cell_features(const CellArgs a, int N, int sorb, float *X) {
   x[12] = (float)(-log10(a.pri_molal[cell]));  // pH proxy: the H+-like first species of the guess
   x[13] = (float)a.temp[cell];
   x[14] = (float)log10(fmax(a.ionic[cell], 1e-30));
+}
+
+// Per-cell features, row-major [cell][kFeat].
+__global__ void cell_features(const CellArgs a, int N, int sorb, float *X) {
+  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (cell >= a.ncells) return;
+  features_of(a, N, sorb, cell, X + cell * kFeat);
+}
+
+// ---------------------------------------------------------------------------
+// Fused inference: features -> 4 layers -> guess in one kernel.  A warp owns
+// 16 rows; the FP32 accumulator tiles of a layer (m16n8) are, two by two,
+// exactly the A fragments (m16k16, BF16) of the next layer for the same
+// lane, so activations never leave the registers.  Weights are read as B
+// fragments pre-packed per (k-chunk, n-tile, lane) -- one coalesced 8-byte
+// load per lane per mma -- from L1/L2, where all warps share them.  The
+// products and their k order are those of gemm_bf16, so the guesses equal the
+// layer-by-layer path's.
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  const __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<const uint32_t *>(&v);
+}
+
+// Packs W [K][Nn] (BF16) into B fragments: u32 index ((kc*NT + nt)*32 + lane)*2 + r.
+__global__ void pack_b_fragments(const bf16 *W, int K, int Nn, uint32_t *out) {
+  const int NT = Nn / 8, KC = K / 16;
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= (long long)KC * NT * 64) return;
+  const int r = (int)(i & 1), lane = (int)((i >> 1) & 31);
+  const long long q = i >> 6;
+  const int nt = (int)(q % NT), kc = (int)(q / NT);
+  const int g = lane >> 2, t = lane & 3;
+  const int k = kc * 16 + 2 * t + 8 * r, n = nt * 8 + g;
+  const bf16 lo = W[(long long)k * Nn + n], hi = W[(long long)(k + 1) * Nn + n];
+  out[i] = (uint32_t)(*reinterpret_cast<const uint16_t *>(&lo)) |
+           ((uint32_t)(*reinterpret_cast<const uint16_t *>(&hi)) << 16);
+}
+
+struct FusedMLP {
+  const uint2 *w1, *w2, *w3, *w4;  // packed B fragments per layer
+  const float *b1, *b2, *b3, *b4;  // FP32 biases
+  const float *fmu, *fisd, *tmu, *tsd;
+};
+
+// One hidden layer of 256 -> 256 for the warp's 16 rows: A fragments in ain
+// (16 k-chunks x 4), GELU activations out as the next A fragments.
+__device__ __forceinline__ void hidden_layer(const uint32_t (&ain)[16][4], uint32_t (&aout)[16][4],
+                                             const uint2 *__restrict__ w, const float *__restrict__ b, int lane) {
+  const int t = lane & 3;
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+#pragma unroll
+    for (int kc = 0; kc < 16; ++kc) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const uint2 bb = __ldg(&w[(kc * 32 + half * 16 + j) * 32 + lane]);
+        const uint32_t bf[2] = {bb.x, bb.y};
+        mma16816(acc[j], ain[kc], bf);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      const int c0 = (half * 16 + j) * 8 + 2 * t, c1 = c0 + 8;
+      const float b00 = __ldg(&b[c0]), b01 = __ldg(&b[c0 + 1]), b10 = __ldg(&b[c1]), b11 = __ldg(&b[c1 + 1]);
+      uint32_t *o = aout[half * 8 + j / 2];
+      o[0] = pack_bf16(gelu(acc[j][0] + b00), gelu(acc[j][1] + b01));
+      o[1] = pack_bf16(gelu(acc[j][2] + b00), gelu(acc[j][3] + b01));
+      o[2] = pack_bf16(gelu(acc[j + 1][0] + b10), gelu(acc[j + 1][1] + b11));
+      o[3] = pack_bf16(gelu(acc[j + 1][2] + b10), gelu(acc[j + 1][3] + b11));
+    }
+  }
+}
+
+__global__ void __launch_bounds__(128) mlp_infer_fused(const CellArgs a, int N, int sorb, FusedMLP p, double *guess) {
+  __shared__ float xs[4][16][kFeat + 1];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int g = lane >> 2, t = lane & 3;
+  const long long nc = a.ncells;
+  const long long row0 = (blockIdx.x * 4LL + warp) * 16;
+  if (row0 >= nc) return;
+  // features of the warp's 16 rows, standardised as standardize() does
+  if (lane < 16) {
+    float x[kFeat];
+    const long long cell = row0 + lane;
+    if (cell < nc) {
+      features_of(a, N, sorb, cell, x);
+      for (int j = 0; j < kFeat; ++j) x[j] = (x[j] - p.fmu[j]) * p.fisd[j];
+    } else {
+      for (int j = 0; j < kFeat; ++j) x[j] = 0.f;
+    }
+    for (int j = 0; j < kFeat; ++j) xs[warp][lane][j] = x[j];
+  }
+  __syncwarp();
+  uint32_t ax[4];
+  ax[0] = pack_bf16(xs[warp][g][2 * t], xs[warp][g][2 * t + 1]);
+  ax[1] = pack_bf16(xs[warp][g + 8][2 * t], xs[warp][g + 8][2 * t + 1]);
+  ax[2] = pack_bf16(xs[warp][g][2 * t + 8], xs[warp][g][2 * t + 9]);
+  ax[3] = pack_bf16(xs[warp][g + 8][2 * t + 8], xs[warp][g + 8][2 * t + 9]);
+  // layer 1: 16 -> 256
+  uint32_t h1[16][4], h2[16][4];
+#pragma unroll
+  for (int half = 0; half < 2; ++half) {
+    float acc[16][4];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      acc[j][0] = acc[j][1] = acc[j][2] = acc[j][3] = 0.f;
+      const uint2 bb = __ldg(&p.w1[(half * 16 + j) * 32 + lane]);
+      const uint32_t bf[2] = {bb.x, bb.y};
+      mma16816(acc[j], ax, bf);
+    }
+#pragma unroll
+    for (int j = 0; j < 16; j += 2) {
+      const int c0 = (half * 16 + j) * 8 + 2 * t, c1 = c0 + 8;
+      const float b00 = __ldg(&p.b1[c0]), b01 = __ldg(&p.b1[c0 + 1]), b10 = __ldg(&p.b1[c1]),
+                  b11 = __ldg(&p.b1[c1 + 1]);
+      uint32_t *o = h1[half * 8 + j / 2];
+      o[0] = pack_bf16(gelu(acc[j][0] + b00), gelu(acc[j][1] + b01));
+      o[1] = pack_bf16(gelu(acc[j][2] + b00), gelu(acc[j][3] + b01));
+      o[2] = pack_bf16(gelu(acc[j + 1][0] + b10), gelu(acc[j + 1][1] + b11));
+      o[3] = pack_bf16(gelu(acc[j + 1][2] + b10), gelu(acc[j + 1][3] + b11));
+    }
+  }
+  hidden_layer(h1, h2, p.w2, p.b2, lane);  // layer 2
+  hidden_layer(h2, h1, p.w3, p.b3, lane);  // layer 3
+  // layer 4: 256 -> kOut (2 n-tiles), no activation
+  float y[2][4];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) y[j][0] = y[j][1] = y[j][2] = y[j][3] = 0.f;
+#pragma unroll
+  for (int kc = 0; kc < 16; ++kc)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const uint2 bb = __ldg(&p.w4[(kc * 2 + j) * 32 + lane]);
+      const uint32_t bf[2] = {bb.x, bb.y};
+      mma16816(y[j], h1[kc], bf);
+    }
+  // outputs -> alternative guess (as outputs_to_guess)
+#pragma unroll
+  for (int j = 0; j < 2; ++j)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int c = j * 8 + 2 * t + (q & 1);
+      const long long cell = row0 + g + (q >= 2 ? 8 : 0);
+      if (c < N && cell < nc) {
+        const float z = y[j][q] + __ldg(&p.b4[c]);
+        const double lm = (double)p.tmu[c] + (double)p.tsd[c] * (double)z;
+        guess[c * nc + cell] = exp(fmin(fmax(lm, -700.0), 700.0));
+      }
+    }
 }
 
 __global__ void standardize(const float *X, const float *mu, const float *sd, bf16 *Xb, long long rows, int cols) {
@@ -275,6 +424,7 @@ struct Surrogate {
   double *guess = nullptr;
   long long guess_cap = 0;
   int steps = 0;
+  uint32_t *wpk = nullptr;  // B-fragment packing of the BF16 weights (fused inference)
 };
 
 namespace {
@@ -381,6 +531,7 @@ Surrogate *surrogate_create(int N, uint64_t seed, std::string *err) {
   if (e == cudaSuccess) e = cudaMalloc(&s->m1, off * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->m2, off * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->wb, off * sizeof(bf16));
+  if (e == cudaSuccess) e = cudaMalloc(&s->wpk, off * sizeof(bf16));
   if (e == cudaSuccess) e = cudaMalloc(&s->fmu, 2 * kFeat * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->tmu, 2 * kOut * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->loss, sizeof(float));
@@ -412,6 +563,7 @@ void surrogate_destroy(Surrogate *s) {
   cudaFree(s->m1);
   cudaFree(s->m2);
   cudaFree(s->wb);
+  cudaFree(s->wpk);
   cudaFree(s->fmu);
   cudaFree(s->tmu);
   cudaFree(s->loss);
@@ -526,13 +678,42 @@ double *surrogate_guess_buffer(Surrogate *s) { return s->guess; }
 // surrogate_prepare.
 cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st) {
   const long long nc = a.ncells;
+  // refresh the B-fragment packing of the current weights (140k values)
+  uint32_t *pk[kLayers];
+  for (int l = 0; l < kLayers; ++l) {
+    pk[l] = s->wpk + s->woff[l] / 2;  // woff is even: every K x N block has an even size
+    const int K = s->dims[l], Nn = s->dims[l + 1];
+    pack_b_fragments<<<blocks((long long)(K / 16) * (Nn / 8) * 64, 256), 256, 0, st>>>(s->wb + s->woff[l], K, Nn, pk[l]);
+  }
+  FusedMLP p;
+  p.w1 = reinterpret_cast<const uint2 *>(pk[0]);
+  p.w2 = reinterpret_cast<const uint2 *>(pk[1]);
+  p.w3 = reinterpret_cast<const uint2 *>(pk[2]);
+  p.w4 = reinterpret_cast<const uint2 *>(pk[3]);
+  p.b1 = s->w + s->boff[0];
+  p.b2 = s->w + s->boff[1];
+  p.b3 = s->w + s->boff[2];
+  p.b4 = s->w + s->boff[3];
+  p.fmu = s->fmu;
+  p.fisd = s->fsd;
+  p.tmu = s->tmu;
+  p.tsd = s->tsd;
+  mlp_infer_fused<<<blocks(nc, 64), 128, 0, st>>>(a, n.N, (n.Nix + n.Nsr) > 0, p, s->guess);
+  return cudaGetLastError();
+}
+
+// The layer-by-layer inference path (GEMM kernels, HBM round trips between
+// layers) into `guess`: kept to check the fused kernel against.
+cudaError_t surrogate_predict_layers(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess,
+                                     cudaStream_t st) {
+  const long long nc = a.ncells;
   cudaError_t e = surrogate_features(n, a, s->feat, st);
   if (e != cudaSuccess) return e;
   for (long long r0 = 0; r0 < nc; r0 += kChunk) {
     const long long rows = std::min(kChunk, nc - r0);
     standardize<<<blocks(rows * kFeat, 256), 256, 0, st>>>(s->feat + r0 * kFeat, s->fmu, s->fsd, s->xb, rows, kFeat);
     forward(s, rows, st, false);
-    outputs_to_guess<<<blocks(rows, 128), 128, 0, st>>>(s->y, kOut, s->tmu, s->tsd, n.N, rows, r0, nc, s->guess);
+    outputs_to_guess<<<blocks(rows, 128), 128, 0, st>>>(s->y, kOut, s->tmu, s->tsd, n.N, rows, r0, nc, guess);
   }
   return cudaGetLastError();
 }

@@ -91,6 +91,7 @@ def _surrogate_bind(l):
     l.pfchem_surrogate_fit.argtypes = [vp, vp, vp, C.c_int64, C.POINTER(SurrogateConfig),
                                        C.POINTER(SurrogateReport)]
     l.pfchem_surrogate_enable.argtypes = [vp, C.c_int]
+    l.pfchem_surrogate_predict_layers.argtypes = [vp, C.POINTER(abi.Cells), vp]
     l.pfchem_surrogate_predict.argtypes = [vp, C.POINTER(abi.Cells), vp]
     l.pfchem_surrogate_gradients.argtypes = [vp, vp, vp, C.c_int64, vp, vp]
     l.pfchem_surrogate_gradients.restype = C.c_int64
@@ -128,6 +129,16 @@ class WarmStartMixin:
         s = cells.struct()
         self._check(self._lib.pfchem_surrogate_predict(self._ctx, C.byref(s), C.c_void_p(g.data_ptr())),
                     "pfchem_surrogate_predict")
+        return g
+
+    def surrogate_predict_layers(self, cells):
+        """The layer-by-layer (GEMM per layer) prediction, to check the fused kernel."""
+        import torch
+        _surrogate_bind(self._lib)
+        g = torch.empty(self.network.N * cells.ncells, dtype=torch.float64, device="cuda")
+        s = cells.struct()
+        self._check(self._lib.pfchem_surrogate_predict_layers(self._ctx, C.byref(s), C.c_void_p(g.data_ptr())),
+                    "pfchem_surrogate_predict_layers")
         return g
 
     def surrogate_enable(self, on=True):

@@ -49,6 +49,24 @@ def test_gradients_match_fp64_oracle():
             assert rel < 2e-2, (l, size, rel)
 
 
+def test_fused_inference_equals_layer_by_layer():
+    """The one-kernel inference (activations in registers, packed weight
+    fragments) computes the same products in the same order as the
+    GEMM-per-layer path: the guesses agree bit for bit, over a batch whose
+    size is not a multiple of the kernel's 64-row tile."""
+    net = workloads.synthetic_network()
+    _, opt, _, _ = workloads.synthetic_cells(8, seed=1, net=net)
+    step = ReactionStep(net, opt)
+    X, molal = _data(step, 65536, 43)
+    fit(step, X, molal, epochs=2, batch=4096)
+    _, _, cells, _ = workloads.synthetic_cells(50001, seed=44, net=net)
+    d = cells.to_device()
+    a = step.surrogate_predict(d).cpu().numpy()
+    b = step.surrogate_predict_layers(d).cpu().numpy()
+    assert np.isfinite(a).all()
+    np.testing.assert_array_equal(a, b)
+
+
 def test_trained_warm_start_reduces_iterations_with_identical_results(oracle):
     net = workloads.synthetic_network()
     _, opt, _, dt = workloads.synthetic_cells(8, seed=1, net=net)
