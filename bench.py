@@ -213,7 +213,7 @@ def main():
             restore()
             step.react(dev, dt)
         torch.cuda.synchronize()
-        dev_ms, iters, alt, slots = [], [], [], []
+        dev_ms, iters, alt, slots, drains = [], [], [], [], []
         with Clocks(clk_index) as clk:
             for _ in range(args.steps):
                 restore()
@@ -226,12 +226,15 @@ def main():
                 iters.append(st.sum_iterations)
                 alt.append(st.alt_guess_used)
                 slots.append(st.lane_slots)
+                drains.append(st.drain_ms)
                 torch.cuda.synchronize()
         eff = float(np.sum(iters)) / float(np.sum(slots)) if np.sum(slots) else None
+        timed.drain_ms = float(np.mean(drains))
         return float(np.sum(dev_ms)), iters, alt, clk.summary(), eff
 
     # plain Newton from the previous-step guess
     plain_ms, plain_iters, _, plain_clocks, plain_eff = timed(local)
+    plain_drain = timed.drain_ms
     plain_value = world * n / (plain_ms / args.steps * 1e-3)
     g_plain = dev.to_host()
     warm = None
@@ -262,6 +265,7 @@ def main():
                     err0_rms=float(err0.pow(2).mean().sqrt()), err0_p50=float(err0.max(0).values.median()))
     total_ms, iters, alt, clocks, eff = (timed(local) if warm is not None
                                          else (plain_ms, plain_iters, [0], plain_clocks, plain_eff))
+    drain = timed.drain_ms if warm is not None else plain_drain
     launch = step.launch()
     g = dev.to_host()
     exact = None
@@ -285,7 +289,7 @@ def main():
             exact[mode] = {"value": world * n / (ms / args.steps * 1e-3), "ms_per_step": ms / args.steps,
                            "mean_newton_iterations": float(np.mean(its)) / n,
                            "max_newton_iterations": int(ge.iterations.max()),
-                           "lane_efficiency": e_eff,
+                           "lane_efficiency": e_eff, "queue_drain_ms": timed.drain_ms,
                            "nonconverged": int((ge.status != 0).sum()),
                            "total_rel_diff_vs_reference_jacobian_max": float(rel[:, both].max())}
         if warm is not None:
@@ -354,7 +358,7 @@ def main():
         r = warm["report"]
         wline = {"plain_value": plain_value, "plain_ms_per_step": plain_ms / args.steps,
                  "plain_mean_newton_iterations": float(np.mean(plain_iters)) / n,
-                 "plain_lane_efficiency": plain_eff,
+                 "plain_lane_efficiency": plain_eff, "plain_queue_drain_ms": plain_drain,
                  "speedup_vs_plain": value / plain_value,
                  "alt_guess_used_frac": float(np.mean(alt)) / n,
                  "surrogate": {"arch": "16-256-256-256-12 GELU MLP, BF16 weights/activations, FP32 accumulate "
@@ -377,7 +381,7 @@ def main():
                               "refill_min_idle": launch.refill_min_idle},
                    "parallelism": "replicas" if world > 1 else "single"},
         "mean_newton_iterations": mean_iters, "converged_cells": conv,
-        "lane_efficiency": eff,
+        "lane_efficiency": eff, "queue_drain_ms": drain,
         "iteration_histogram": np.bincount(g.iterations).tolist(),
         "gpu_launches": args.steps * (1 if warm is None else 2 + 6 * ((n + 262143) // 262144)),
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": probe, "unit": "TFLOP/s",

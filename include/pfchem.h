@@ -231,6 +231,9 @@ typedef struct pfchem_stats {
   int64_t lane_slots;      /* 32 x warp trips of Newton steps in the persistent
                               kernel: sum_iterations / lane_slots is the share
                               of SIMT lanes doing Newton work (0 if not counted) */
+  double drain_ms;         /* time from the work queue running dry to the
+                              last warp's exit: the straggler tail (0 if not
+                              measured) */
 } pfchem_stats;
 
 typedef struct pfchem_ctx pfchem_ctx;

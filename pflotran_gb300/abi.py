@@ -111,7 +111,7 @@ class Stats(C.Structure):
     _fields_ = [
         ("ncells", C.c_int64), ("sum_iterations", C.c_int64), ("max_iterations", C.c_int32),
         ("nonconverged", C.c_int32), ("alt_guess_used", C.c_int64), ("kernel_ms", C.c_double),
-        ("lane_slots", C.c_int64),
+        ("lane_slots", C.c_int64), ("drain_ms", C.c_double),
     ]
 
 

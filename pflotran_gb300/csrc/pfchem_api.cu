@@ -50,7 +50,9 @@ cudaError_t surrogate_get_params(Surrogate *s, float *host);
 cudaError_t surrogate_set_params(Surrogate *s, const float *host);
 cudaError_t surrogate_prepare(Surrogate *s, long long ncells);
 double *surrogate_guess_buffer(Surrogate *s);
-cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st);
+cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess, cudaStream_t st,
+                              bool pack = true);
+cudaError_t surrogate_pack(Surrogate *s, cudaStream_t st);
 cudaError_t surrogate_predict_layers(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess,
                                      cudaStream_t st);
 cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, float *T, cudaStream_t st);
@@ -316,6 +318,11 @@ int default_specialized_launch(pfchem_ctx *c) {
   return 0;
 }
 
+double drain_ms(const Scratch &h) {
+  const unsigned long long t0 = ~h.t_drain_inv;
+  return (h.t_drain_inv && h.t_end > t0) ? (double)(h.t_end - t0) * 1e-6 : 0.0;
+}
+
 int check_cells(pfchem_ctx *c, const pfchem_cells *cl) {
   if (!c || !cl) return fail(c, -1, "null argument");
   if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
@@ -387,18 +394,22 @@ int reserve_prep(pfchem_ctx *c, int64_t ncells) {
 // Enqueues one reaction step on `st`: statistics reset, warm-start inference
 // (when `predict`; a.alt_guess must then point at the surrogate's guess
 // buffer), the prologue and the persistent solve.  Allocates nothing.
-int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st) {
+int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st, Scratch *scr = nullptr,
+                 double *prep = nullptr, bool pack = true) {
   const DevNet &n = c->net;
   const pfchem_launch &L = c->launch;
   const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
-  cudaError_t me = cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), st);
+  if (!scr) scr = c->scratch;
+  if (!prep) prep = c->prep;
+  cudaError_t me = cudaMemsetAsync(scr, 0, sizeof(Scratch), st);
   if (me != cudaSuccess) return fail(c, -2, "statistics reset: %s", cudaGetErrorString(me));
-  cudaError_t pe = predict ? surrogate_predict(c->sur, n, a, st) : cudaSuccess;
+  cudaError_t pe =
+      predict ? surrogate_predict(c->sur, n, a, const_cast<double *>(a.alt_guess), st, pack) : cudaSuccess;
   if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
   cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
-                       ? gen_launch(c->gen_fn, c->gen_pro, n, a, c->scratch, c->prep, grid, L.block_threads,
+                       ? gen_launch(c->gen_fn, c->gen_pro, n, a, scr, prep, grid, L.block_threads,
                                     L.refill_min_idle, st)
-                       : launch_react(n, a, c->scratch, grid, L.block_threads, L.refill_min_idle, st);
+                       : launch_react(n, a, scr, grid, L.block_threads, L.refill_min_idle, st);
   if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
   return 0;
 }
@@ -456,6 +467,7 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
   c->stats.alt_guess_used = (int64_t)h.alt_used;
   c->stats.kernel_ms = ms;
   c->stats.lane_slots = 32 * (int64_t)h.newton_trips;
+  c->stats.drain_ms = drain_ms(h);
   return (int)h.nonconverged;
 }
 
@@ -699,6 +711,7 @@ int pfchem_async_stats(pfchem_ctx *c, pfchem_stats *s) {
   s->alt_guess_used = (int64_t)h.alt_used;
   s->kernel_ms = 0.0;
   s->lane_slots = 32 * (int64_t)h.newton_trips;
+  s->drain_ms = drain_ms(h);
   return 0;
 }
 
@@ -1017,7 +1030,7 @@ int pfchem_surrogate_predict(pfchem_ctx *c, pfchem_cells *cl, double *guess) {
   CellArgs a = device_args(cl, 1.0);
   if (a.ncells == 0) return 0;
   CUDA_TRY(c, surrogate_prepare(c->sur, a.ncells));
-  CUDA_TRY(c, surrogate_predict(c->sur, c->net, a, c->stream));
+  CUDA_TRY(c, surrogate_predict(c->sur, c->net, a, surrogate_guess_buffer(c->sur), c->stream));
   CUDA_TRY(c, cudaMemcpyAsync(guess, surrogate_guess_buffer(c->sur), (size_t)c->net.N * a.ncells * sizeof(double),
                               cudaMemcpyDeviceToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));

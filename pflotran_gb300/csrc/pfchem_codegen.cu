@@ -156,6 +156,8 @@ struct Gen {
     o << "typedef long long int64_t;\ntypedef int int32_t;\n";
     o << "struct CellArgs { " PFCHEM_STR(PFCHEM_CELLARGS_FIELDS) " };\n";
     o << "struct Scratch { " PFCHEM_STR(PFCHEM_SCRATCH_FIELDS) " };\n";
+    o << "__device__ __forceinline__ unsigned long long pf_now() { unsigned long long t; "
+         "asm volatile(\"mov.u64 %0, %%globaltimer;\" : \"=l\"(t)); return t; }\n";
     o << "#define NP " << n.N << "\n#define NC " << (n.Nc > 0 ? n.Nc : 1) << "\n#define NM "
       << (n.Nm > 0 ? n.Nm : 1) << "\n#define NIX " << (n.Nix > 0 ? n.Nix : 1) << "\n#define NSR "
       << (n.Nsr > 0 ? n.Nsr : 1) << "\n#define NSC " << (n.Nsc > 0 ? n.Nsc : 1) << "\n#define JS " << js << "\n"
@@ -895,6 +897,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
             load_prep(L, a, cell, prep, inv_dt);
           }
         } else {
+          if (!exhausted) atomicMax(&scr->t_drain_inv, ~pf_now());
           exhausted = true;
         }
       }
@@ -925,6 +928,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   if (lane == 0) {
     atomicAdd(&scr->sum_iter, my_iters);
     atomicAdd(&scr->newton_trips, my_trips);
+    atomicMax(&scr->t_end, pf_now());
     (void)my_alt;
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);

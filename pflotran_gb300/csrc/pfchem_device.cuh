@@ -86,6 +86,8 @@ struct DevNet {
   unsigned long long sum_iter;                        \
   unsigned long long alt_used;                        \
   unsigned long long newton_trips; /* warp trips of Newton steps */ \
+  unsigned long long t_drain_inv;  /* ~(first time the queue ran dry), ns */ \
+  unsigned long long t_end;        /* last warp exit, ns */ \
   unsigned int max_iter;                              \
   unsigned int nonconverged;
 
@@ -96,6 +98,11 @@ struct CellArgs {
 struct Scratch {
   PFCHEM_SCRATCH_FIELDS
 };
+
+// global nanosecond timer (queue-drain statistics only)
+#define PFCHEM_GLOBALTIMER_FN \
+  __device__ __forceinline__ unsigned long long pf_now() { \
+    unsigned long long t; asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)); return t; }
 
 #define PFCHEM_STR_(...) #__VA_ARGS__
 #define PFCHEM_STR(...) PFCHEM_STR_(__VA_ARGS__)

@@ -672,19 +672,29 @@ cudaError_t surrogate_prepare(Surrogate *s, long long ncells) {
 
 double *surrogate_guess_buffer(Surrogate *s) { return s->guess; }
 
-// Inference for a batch of cells: features -> MLP -> alternative guess in the
-// surrogate's guess buffer (device SoA, [N][ncells]).  Launch-only (no
+// Inference for a batch of cells: features -> MLP -> alternative guess into
+// `guess` (device SoA, [N][ncells]; normally the surrogate's guess buffer).  Launch-only (no
 // allocation, no synchronisation): capturable in a CUDA graph after
 // surrogate_prepare.
-cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, cudaStream_t st) {
-  const long long nc = a.ncells;
-  // refresh the B-fragment packing of the current weights (140k values)
-  uint32_t *pk[kLayers];
+// Refreshes the B-fragment packing of the current weights (140k values).
+cudaError_t surrogate_pack(Surrogate *s, cudaStream_t st) {
   for (int l = 0; l < kLayers; ++l) {
-    pk[l] = s->wpk + s->woff[l] / 2;  // woff is even: every K x N block has an even size
     const int K = s->dims[l], Nn = s->dims[l + 1];
-    pack_b_fragments<<<blocks((long long)(K / 16) * (Nn / 8) * 64, 256), 256, 0, st>>>(s->wb + s->woff[l], K, Nn, pk[l]);
+    pack_b_fragments<<<blocks((long long)(K / 16) * (Nn / 8) * 64, 256), 256, 0, st>>>(
+        s->wb + s->woff[l], K, Nn, s->wpk + s->woff[l] / 2);  // woff is even: every K x N block is
   }
+  return cudaGetLastError();
+}
+
+cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess, cudaStream_t st,
+                              bool pack) {
+  const long long nc = a.ncells;
+  if (pack) {
+    cudaError_t e = surrogate_pack(s, st);
+    if (e != cudaSuccess) return e;
+  }
+  uint32_t *pk[kLayers];
+  for (int l = 0; l < kLayers; ++l) pk[l] = s->wpk + s->woff[l] / 2;
   FusedMLP p;
   p.w1 = reinterpret_cast<const uint2 *>(pk[0]);
   p.w2 = reinterpret_cast<const uint2 *>(pk[1]);
@@ -698,7 +708,7 @@ cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, 
   p.fisd = s->fsd;
   p.tmu = s->tmu;
   p.tsd = s->tsd;
-  mlp_infer_fused<<<blocks(nc, 64), 128, 0, st>>>(a, n.N, (n.Nix + n.Nsr) > 0, p, s->guess);
+  mlp_infer_fused<<<blocks(nc, 64), 128, 0, st>>>(a, n.N, (n.Nix + n.Nsr) > 0, p, guess);
   return cudaGetLastError();
 }
 

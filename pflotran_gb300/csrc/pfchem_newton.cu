@@ -70,6 +70,7 @@ struct Lane {
 };
 
 __device__ __forceinline__ double sgn1(double x) { return signbit(x) ? -1.0 : 1.0; }
+PFCHEM_GLOBALTIMER_FN
 
 // LAG activity coefficients at ionic strength I (reaction.F90:3992-4051), as
 // ln gamma; complexes fold theirs into bc = bK - ln gamma.
@@ -682,6 +683,7 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
             if (a.alt_guess) arm_alt_guess(n, a, cell, L);
           }
         } else {
+          if (!exhausted) atomicMax(&scr->t_drain_inv, ~pf_now());
           exhausted = true;
         }
       }
@@ -724,6 +726,7 @@ __global__ void __launch_bounds__(256) react_kernel(const __grid_constant__ DevN
   if (lane == 0) {
     atomicAdd(&scr->sum_iter, my_iters);
     atomicAdd(&scr->newton_trips, my_trips);
+    atomicMax(&scr->t_end, pf_now());
     atomicAdd(&scr->alt_used, my_alt);
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);

@@ -352,3 +352,32 @@ def test_constraint_speciation(oracle):
     assert ok.sum() >= cells.ncells - max(bad, bad_ref) - 2
     assert np.mean(g.iterations[ok] == ref.iterations[ok]) > 0.98
     assert_parity(net, g, ref, mask=ok)
+
+
+@pytest.mark.parametrize("warm", [False, True])
+def test_large_host_batch_equals_device_batch(warm):
+    """A host-pointer batch of 2^20 cells (staged through the device) gives
+    every cell the device batch's result, bit for bit, with and without the
+    warm start."""
+    from pflotran_gb300.surrogate import fit, generate
+    net = workloads.synthetic_network()
+    _, opt, cells, dt = workloads.synthetic_cells(1 << 20, seed=51, net=net, device="cuda")
+    step = ReactionStep(net, opt)
+    if warm:
+        X, molal = generate(step, lambda m, s: workloads.synthetic_cells(m, seed=s, net=net, device="cuda")[2],
+                            131072, 52, dt, chunk=131072)
+        fit(step, X, molal, epochs=2, batch=4096)
+        step.surrogate_enable(True)
+    d = cells.to_device()
+    step.react(d, dt)
+    st_dev = step.stats()
+    g_dev = d.to_host()
+    h = cells.copy()
+    step.react(h, dt)
+    st_host = step.stats()
+    for f in ("pri_molal", "total_out", "mnrl_rate", "mnrl_volfrac", "total_sorb_eq", "ionic_strength",
+              "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc", "iterations", "status"):
+        np.testing.assert_array_equal(getattr(h, f), getattr(g_dev, f), err_msg=f)
+    assert st_host.sum_iterations == st_dev.sum_iterations
+    assert st_host.nonconverged == st_dev.nonconverged
+    assert st_host.alt_guess_used == st_dev.alt_guess_used
