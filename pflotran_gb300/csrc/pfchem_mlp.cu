@@ -200,19 +200,23 @@ __global__ void to_bf16(const float *x, bf16 *y, long long n) {
 }
 
 // Per-cell features (raw, before standardisation) of one cell into x[kFeat].
+// The conserved totals are formed in FP64; the logarithms are taken in FP32,
+// which is far finer than the BF16 the network reads them in (and keeps the
+// FP64 pipe for the Newton work).
 __device__ __forceinline__ void features_of(const CellArgs &a, int N, int sorb, long long cell, float *x) {
   const long long nc = a.ncells;
   const double por = a.por[cell], sat = a.sat[cell], vol = a.vol[cell];
   const double psv = por * sat * 1000.0 * vol;
+  const double ipsv = 1e12 / psv;
   for (int j = 0; j < kFeat; ++j) x[j] = 0.f;
   for (int j = 0; j < N; ++j) {
     double acc = psv * a.total[j * a.total_stride_comp + cell * a.total_stride_cell];
     if (sorb) acc += vol * a.sorb[j * nc + cell];
-    x[j] = (float)asinh(acc / psv * 1e12);  // signed log of the conserved total [mol/L pore water]
+    x[j] = asinhf((float)(acc * ipsv));  // signed log of the conserved total [mol/L pore water]
   }
-  x[12] = (float)(-log10(a.pri_molal[cell]));  // pH proxy: the H+-like first species of the guess
+  x[12] = -log10f(fmaxf((float)a.pri_molal[cell], 1e-37f));  // pH proxy: the H+-like first species of the guess
   x[13] = (float)a.temp[cell];
-  x[14] = (float)log10(fmax(a.ionic[cell], 1e-30));
+  x[14] = log10f(fmaxf((float)a.ionic[cell], 1e-30f));
 }
 
 // Per-cell features, row-major [cell][kFeat].
