@@ -57,6 +57,8 @@ def parse():
     p.add_argument("--plain-only", action="store_true")
     p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
                    help="also time the step with the exact Newton Jacobian")
+    p.add_argument("--jacobian", choices=("reference", "exact"), default="reference",
+                   help="Newton Jacobian of the headline run")
     return p.parse_args()
 
 
@@ -194,6 +196,10 @@ def main():
     from pflotran_gb300.lib import ReactionStep
 
     net, opt, host, dt = make_workload(args.ncells, device=f"cuda:{local}", rank=rank)
+    if args.jacobian == "exact":
+        from pflotran_gb300 import abi as _abi
+        opt.jacobian = _abi.JACOBIAN_EXACT
+        args.exact_jacobian = False  # the headline already is the exact-Jacobian run
     n = host.ncells
     step = ReactionStep(net, opt, device=local)
     pristine = host.to_device()
@@ -399,6 +405,8 @@ def main():
     }
     if exact is not None:
         line["exact_jacobian"] = exact
+    if args.jacobian == "exact":
+        line["config"]["workload"] += ", exact Newton Jacobian (PFCHEM_JACOBIAN_EXACT)"
     if wline is not None:
         line["warm_start"] = wline
         line["config"]["workload"] = line["config"]["workload"].replace(

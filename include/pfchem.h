@@ -389,6 +389,8 @@ typedef struct pfchem_launch {
 } pfchem_launch;
 #define PFCHEM_KERNEL_SPECIALIZED 0 /* network-specialized kernel compiled at set_network (default) */
 #define PFCHEM_KERNEL_GENERIC 1     /* table-driven kernel compiled into the library */
+#define PFCHEM_KERNEL_SPECIALIZED_COMPACT 2 /* specialized, J alone in shared memory (right-hand
+                                               side in registers): fits more blocks per SM, same results */
 int pfchem_get_launch(const pfchem_ctx *ctx, pfchem_launch *launch);
 int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
 /* Times candidate mappings on `cells` (device pointers; the state arrays are

@@ -40,6 +40,7 @@ CELL_INACTIVE = 5
 
 KERNEL_SPECIALIZED = 0
 KERNEL_GENERIC = 1
+KERNEL_SPECIALIZED_COMPACT = 2
 JACOBIAN_REFERENCE = 0
 JACOBIAN_EXACT = 1
 

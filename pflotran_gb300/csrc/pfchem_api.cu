@@ -29,13 +29,13 @@ cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mi
 cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
                                    double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
-int gen_kernel(const DevNet &n, int block, void **fn_out, void **pro_out, std::string *err);
+int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **pro_out, std::string *err);
 int gen_prep_fields(const DevNet &n);
-int gen_blocks_per_sm(void *fn, const DevNet &n, int block);
-size_t gen_shared_bytes(const DevNet &n, int block);
-std::string generate_source(const DevNet &n, int block);
+int gen_blocks_per_sm(void *fn, const DevNet &n, int block, bool compact);
+size_t gen_shared_bytes(const DevNet &n, int block, bool compact);
+std::string generate_source(const DevNet &n, int block, bool compact);
 cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, Scratch *scr, double *prep, int grid,
-                       int block, int refill, cudaStream_t st);
+                       int block, int refill, cudaStream_t st, bool compact);
 struct Surrogate;
 Surrogate *surrogate_create(int N, uint64_t seed, std::string *err);
 void surrogate_destroy(Surrogate *s);
@@ -88,6 +88,7 @@ struct pfchem_ctx {
   void *gen_fn = nullptr;  // specialized kernel for gen_block threads per block
   void *gen_pro = nullptr; // its data-parallel prologue
   int gen_block = 0;
+  bool gen_compact = false;  // its shared-memory layout (PFCHEM_KERNEL_SPECIALIZED_COMPACT)
   double *prep = nullptr;  // prologue records, gen_prep_fields x prep_cells doubles
   int64_t prep_cells = 0;
   Surrogate *sur = nullptr;  // learned warm start
@@ -289,27 +290,34 @@ void default_launch(pfchem_ctx *c) {
 
 // Compiles (or reuses) the network-specialized kernel for `block` threads per
 // block and returns its resident blocks per SM (0 on failure, message in err).
-int ensure_gen(pfchem_ctx *c, int block) {
-  if (c->gen_fn && c->gen_block == block) return gen_blocks_per_sm(c->gen_fn, c->net, block);
+bool is_specialized(int v) { return v == PFCHEM_KERNEL_SPECIALIZED || v == PFCHEM_KERNEL_SPECIALIZED_COMPACT; }
+
+int ensure_gen(pfchem_ctx *c, int block, bool compact) {
+  if (c->gen_fn && c->gen_block == block && c->gen_compact == compact)
+    return gen_blocks_per_sm(c->gen_fn, c->net, block, compact);
   std::string e;
   void *fn = nullptr, *pro = nullptr;
-  if (gen_kernel(c->net, block, &fn, &pro, &e) != 0) {
+  if (gen_kernel(c->net, block, compact, &fn, &pro, &e) != 0) {
     fail(c, -2, "specialized kernel: %s", e.c_str());
     return 0;
   }
   c->gen_fn = fn;
   c->gen_pro = pro;
   c->gen_block = block;
-  int nb = gen_blocks_per_sm(fn, c->net, block);
+  c->gen_compact = compact;
+  int nb = gen_blocks_per_sm(fn, c->net, block, compact);
   if (nb < 1) fail(c, -1, "specialized kernel with %d threads per block does not fit on an SM", block);
   return nb;
 }
 
-// Specialized kernel, 32 threads per block, as many blocks per SM as fit,
-// refill when 8 lanes of a warp are idle.
+// Specialized kernel (augmented layout), 32 threads per block, as many
+// blocks per SM as fit, refill when 8 lanes of a warp are idle.  The compact
+// layout fits one more block per SM for the 12-species network but measured
+// 1-4% slower (its unrolled elimination costs more than the extra warp
+// gains); the autotuner tries both.
 int default_specialized_launch(pfchem_ctx *c) {
   const int block = 32;
-  int nb = ensure_gen(c, block);
+  int nb = ensure_gen(c, block, false);
   if (nb < 1) return -2;
   c->launch.block_threads = block;
   c->launch.blocks_per_sm = nb;
@@ -406,9 +414,9 @@ int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st
   cudaError_t pe =
       predict ? surrogate_predict(c->sur, n, a, const_cast<double *>(a.alt_guess), st, pack) : cudaSuccess;
   if (pe != cudaSuccess) return fail(c, -2, "surrogate launch: %s", cudaGetErrorString(pe));
-  cudaError_t le = (L.variant == PFCHEM_KERNEL_SPECIALIZED)
+  cudaError_t le = is_specialized(L.variant)
                        ? gen_launch(c->gen_fn, c->gen_pro, n, a, scr, prep, grid, L.block_threads,
-                                    L.refill_min_idle, st)
+                                    L.refill_min_idle, st, L.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT)
                        : launch_react(n, a, scr, grid, L.block_threads, L.refill_min_idle, st);
   if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
   return 0;
@@ -428,7 +436,7 @@ int run_solve(pfchem_ctx *c, const CellArgs &a_in) {
     a.alt_guess = surrogate_guess_buffer(c->sur);
   }
   const pfchem_launch &L = c->launch;
-  if (L.variant == PFCHEM_KERNEL_SPECIALIZED) {
+  if (is_specialized(L.variant)) {
     const int re = reserve_prep(c, a.ncells);
     if (re) return re;
   }
@@ -612,8 +620,8 @@ int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_op
     // the network-specialized kernel is the default; a compile failure is an error
     default_launch(c);
     if (default_specialized_launch(c) != 0) return -2;
-  } else if (c->launch.variant == PFCHEM_KERNEL_SPECIALIZED) {
-    if (ensure_gen(c, c->launch.block_threads) < 1) return -2;
+  } else if (is_specialized(c->launch.variant)) {
+    if (ensure_gen(c, c->launch.block_threads, c->launch.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT) < 1) return -2;
   }
   return 0;
 }
@@ -684,7 +692,7 @@ int pfchem_react_batch_async(pfchem_ctx *c, double dt, pfchem_cells *cl, void *s
   CellArgs a = device_args(cl, dt);
   c->async_cells = a.ncells;
   if (a.ncells == 0) return 0;
-  if (c->launch.variant == PFCHEM_KERNEL_SPECIALIZED && c->prep_cells < a.ncells)
+  if (is_specialized(c->launch.variant) && c->prep_cells < a.ncells)
     return fail(c, -1, "%lld cells exceed the reserved %lld: call pfchem_reserve first", (long long)a.ncells,
                 (long long)c->prep_cells);
   const bool predict = c->sur && c->sur_on && surrogate_trained(c->sur) && !a.alt_guess;
@@ -803,13 +811,14 @@ int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
     return fail(c, -1, "block_threads must be a multiple of 32 in [32, 256]");
   if (l->refill_min_idle < 1 || l->refill_min_idle > 32) return fail(c, -1, "refill_min_idle must be in [1, 32]");
   if (l->blocks_per_sm < 1) return fail(c, -1, "blocks_per_sm must be >= 1");
-  if (l->variant != PFCHEM_KERNEL_SPECIALIZED && l->variant != PFCHEM_KERNEL_GENERIC)
+  if (!is_specialized(l->variant) && l->variant != PFCHEM_KERNEL_GENERIC)
     return fail(c, -1, "unknown kernel variant %d", l->variant);
   if (c->has_net) {
-    if (l->variant == PFCHEM_KERNEL_SPECIALIZED) {
-      if (gen_shared_bytes(c->net, l->block_threads) > 227 * 1024)
+    if (is_specialized(l->variant)) {
+      const bool cmp = l->variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT;
+      if (gen_shared_bytes(c->net, l->block_threads, cmp) > 227 * 1024)
         return fail(c, -1, "block_threads %d needs too much shared memory", l->block_threads);
-      int nb = ensure_gen(c, l->block_threads);
+      int nb = ensure_gen(c, l->block_threads, cmp);
       if (nb < 1) return -2;
       if (l->blocks_per_sm > nb) return fail(c, -1, "at most %d blocks of %d threads fit on an SM", nb, l->block_threads);
     } else {
@@ -858,21 +867,25 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   double best = 1e30;
   pfchem_launch best_l = c->launch;
   int rc = 0;
-  for (int b : blocks) {
-    if (gen_shared_bytes(n, b) > 227 * 1024) continue;
-    int nb = ensure_gen(c, b);
-    if (nb < 1) continue;
-    for (int r : refills) {
-      pfchem_launch l{b, nb, r, PFCHEM_KERNEL_SPECIALIZED};
-      c->launch = l;
-      rc = pfchem_react_batch(c, dt, cl);
-      if (rc < 0) break;
-      const double ms = c->stats.kernel_ms;
-      if (ms < best) {
-        best = ms;
-        best_l = l;
+  for (int variant : {PFCHEM_KERNEL_SPECIALIZED, PFCHEM_KERNEL_SPECIALIZED_COMPACT}) {
+    const bool cmp = variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT;
+    for (int b : blocks) {
+      if (gen_shared_bytes(n, b, cmp) > 227 * 1024) continue;
+      int nb = ensure_gen(c, b, cmp);
+      if (nb < 1) continue;
+      for (int r : refills) {
+        pfchem_launch l{b, nb, r, variant};
+        c->launch = l;
+        rc = pfchem_react_batch(c, dt, cl);
+        if (rc < 0) break;
+        const double ms = c->stats.kernel_ms;
+        if (ms < best) {
+          best = ms;
+          best_l = l;
+        }
+        for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
       }
-      for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+      if (rc < 0) break;
     }
     if (rc < 0) break;
   }
@@ -884,7 +897,9 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   if (rc < 0) return rc;
   c->launch = best_l;
   c->launch_forced = true;
-  if (best_l.variant == PFCHEM_KERNEL_SPECIALIZED && ensure_gen(c, best_l.block_threads) < 1) return -2;
+  if (is_specialized(best_l.variant) &&
+      ensure_gen(c, best_l.block_threads, best_l.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT) < 1)
+    return -2;
   return 0;
 }
 
@@ -1121,19 +1136,26 @@ int pfchem_check_specialized(const pfchem_network *net, const pfchem_options *op
     if (log && loglen) snprintf(log, loglen, "%s", tmp.err);
     return r;
   }
-  const std::string src = generate_source(n, block_threads);
-  nvrtcProgram prog;
-  if (nvrtcCreateProgram(&prog, src.c_str(), "pfchem_gen.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) return -2;
-  const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--fmad=true",
-                        "--ptxas-options=-v"};
-  nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
-  size_t ls = 0;
-  nvrtcGetProgramLogSize(prog, &ls);
-  std::string lg(ls, '\0');
-  nvrtcGetProgramLog(prog, &lg[0]);
-  nvrtcDestroyProgram(&prog);
-  if (log && loglen) snprintf(log, loglen, "%s", lg.c_str());
-  return rc == NVRTC_SUCCESS ? 0 : -2;
+  // both shared-memory layouts (augmented and compact), logs concatenated
+  std::string all;
+  int res = 0;
+  for (int compact = 0; compact < 2; ++compact) {
+    const std::string src = generate_source(n, block_threads, compact != 0);
+    nvrtcProgram prog;
+    if (nvrtcCreateProgram(&prog, src.c_str(), "pfchem_gen.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) return -2;
+    const char *opts[] = {"--gpu-architecture=sm_103a", "--std=c++17", "-default-device", "--fmad=true",
+                          "--ptxas-options=-v"};
+    nvrtcResult rc = nvrtcCompileProgram(prog, 5, opts);
+    size_t ls = 0;
+    nvrtcGetProgramLogSize(prog, &ls);
+    std::string lg(ls, '\0');
+    nvrtcGetProgramLog(prog, &lg[0]);
+    nvrtcDestroyProgram(&prog);
+    all += (compact ? "--- compact layout ---\n" : "--- augmented layout ---\n") + std::string(lg.c_str());
+    if (rc != NVRTC_SUCCESS) res = -2;
+  }
+  if (log && loglen) snprintf(log, loglen, "%s", all.c_str());
+  return res;
 }
 
 }  // extern "C"

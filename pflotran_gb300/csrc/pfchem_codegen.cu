@@ -71,9 +71,11 @@ struct Gen {
   const DevNet &n;
   int js;  // threads per block (shared-memory stride)
   std::ostringstream o;
-  Gen(const DevNet &net, int block) : n(net), js(block) {}
+  bool compact = false;  // J alone in shared memory, the right-hand side in registers
+  Gen(const DevNet &net, int block, bool cmp = false) : n(net), js(block), compact(cmp) {}
 
-  std::string J(int i, int k) const { return "Jb[" + I((i * (n.N + 1) + k) * js) + "]"; }
+  int rs() const { return compact ? n.N : n.N + 1; }  // row stride of the shared-memory system
+  std::string J(int i, int k) const { return "Jb[" + I((i * rs() + k) * js) + "]"; }
   std::string E(int i) const { return "Eb[" + I(i * js) + "]"; }
   // log K part of the complex constants: kept in the lane only when activity
   // coefficients change during the solve (NEWTON_ITER); else folded into bc
@@ -626,6 +628,62 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   // Gaussian elimination with power-of-two implicit-scaling pivoting on the
   // augmented [J | F] (column N holds the right-hand side); solution into x.
   void solve() {
+    if (compact) {
+      // J alone in shared memory: the right-hand side stays in registers
+      // (pivot-column and row loops unrolled so every f index is a constant),
+      // the row exponents are 16-bit.  The same operations in the same
+      // order as the augmented form below.
+      o << R"(__device__ __forceinline__ bool lu_solve(double *Jb, unsigned short *Eb, double (&f)[NP]) {
+#define JA(i, k) Jb[((i) * NP + (k)) * JS]
+#pragma unroll 1
+  for (int i = 0; i < NP; ++i) {
+    long long r = 0;
+    for (int k = 0; k < NP; ++k) { const long long v = absbits(JA(i, k)); r = v > r ? v : r; }
+    if (r == 0) return false;
+    Eb[i * JS] = (unsigned short)((r & 0x7FF0000000000000LL) >> 48);
+  }
+#pragma unroll
+  for (int j = 0; j < NP; ++j) {
+    int p = j;
+    long long best = absbits(JA(j, j)) - ((long long)Eb[j * JS] << 48);
+#pragma unroll
+    for (int i = j + 1; i < NP; ++i) {
+      const long long kk = absbits(JA(i, j)) - ((long long)Eb[i * JS] << 48);
+      if (kk >= best) { best = kk; p = i; }
+    }
+    if (p != j) {
+#pragma unroll 1
+      for (int k = j; k < NP; ++k) { const double t = JA(p, k); JA(p, k) = JA(j, k); JA(j, k) = t; }
+      const unsigned short te = Eb[p * JS]; Eb[p * JS] = Eb[j * JS]; Eb[j * JS] = te;
+#pragma unroll
+      for (int i = j + 1; i < NP; ++i)
+        if (p == i) { const double t = f[i]; f[i] = f[j]; f[j] = t; }
+    }
+    double piv = JA(j, j);
+    if (piv == 0.0) piv = 1e-20;
+    const double ip = 1.0 / piv;
+    JA(j, j) = ip;
+#pragma unroll
+    for (int i = j + 1; i < NP; ++i) {
+      const double l = JA(i, j) * ip;
+#pragma unroll 1
+      for (int k = j + 1; k < NP; ++k) JA(i, k) = fma(-l, JA(j, k), JA(i, k));
+      f[i] = fma(-l, f[j], f[i]);
+    }
+  }
+#pragma unroll
+  for (int i = NP - 1; i >= 0; --i) {
+    double s = f[i];
+#pragma unroll
+    for (int k = i + 1; k < NP; ++k) s = fma(-JA(i, k), f[k], s);
+    f[i] = s * JA(i, i);
+  }
+#undef JA
+  return true;
+}
+)";
+      return;
+    }
     // rolled loops over the shared-memory system keep the code compact; the
     // reciprocal pivots overwrite the diagonal and the solution overwrites
     // the right-hand-side column
@@ -672,7 +730,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
 
   void newton_step() {
     const int N = n.N;
-    o << "__device__ __forceinline__ int newton_step(Lane &L, double *Jb, long long *Eb) {\n";
+    o << "__device__ __forceinline__ int newton_step(Lane &L, double *Jb, " << (compact ? "unsigned short" : "long long")
+      << " *Eb) {\n";
     o << "  L.iter += 1;\n";
     if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) {
       o << "  if (L.iter > 1) {\n  double Iv = L.Iacc;\n";
@@ -693,9 +752,15 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         o << "  }\n";
       }
     }
-    for (int j = 0; j < N; ++j) o << "  " << J(j, N) << " = L.F[" << j << "];\n";
-    o << "  if (!lu_solve(Jb, Eb)) return " << PFCHEM_CELL_SINGULAR << ";\n  double x[NP];\n";
-    for (int j = 0; j < N; ++j) o << "  x[" << j << "] = " << J(j, N) << ";\n";
+    if (compact) {
+      o << "  double x[NP];\n";
+      for (int j = 0; j < N; ++j) o << "  x[" << j << "] = L.F[" << j << "];\n";
+      o << "  if (!lu_solve(Jb, Eb, x)) return " << PFCHEM_CELL_SINGULAR << ";\n";
+    } else {
+      for (int j = 0; j < N; ++j) o << "  " << J(j, N) << " = L.F[" << j << "];\n";
+      o << "  if (!lu_solve(Jb, Eb)) return " << PFCHEM_CELL_SINGULAR << ";\n  double x[NP];\n";
+      for (int j = 0; j < N; ++j) o << "  x[" << j << "] = " << J(j, N) << ";\n";
+    }
     o << "  double mrc = 0.0; bool nf = false; double mnew[NP];\n";
     for (int j = 0; j < N; ++j) {
       if (n.use_log) {
@@ -867,7 +932,10 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     o << "extern \"C\" __global__ void __launch_bounds__(" << js << ") pfchem_gen_react(const __grid_constant__ CellArgs a, "
          "Scratch *scr, int refill_min_idle, double inv_dt, const double *prep) {\n";
     o << "  extern __shared__ double smem[];\n  double *Jb = smem + threadIdx.x;\n";
-    o << "  long long *Eb = (long long *)(smem + " << n.N * (n.N + 1) * js << ") + threadIdx.x;\n";
+    if (compact)
+      o << "  unsigned short *Eb = (unsigned short *)(smem + " << n.N * n.N * js << ") + threadIdx.x;\n";
+    else
+      o << "  long long *Eb = (long long *)(smem + " << n.N * (n.N + 1) * js << ") + threadIdx.x;\n";
     o << R"(  const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   Lane L;
@@ -996,22 +1064,25 @@ std::map<std::string, Loaded> g_cache;  // key: device + block + source
 
 }  // namespace
 
-std::string generate_source(const DevNet &n, int block) {
-  Gen g(n, block);
+std::string generate_source(const DevNet &n, int block, bool compact) {
+  Gen g(n, block, compact);
   return g.source();
 }
 
-size_t gen_shared_bytes(const DevNet &n, int block) {
+// Shared memory of the persistent kernel: per thread the augmented [J | F]
+// and 64-bit row exponents, or (compact) J and 16-bit row exponents.
+size_t gen_shared_bytes(const DevNet &n, int block, bool compact) {
+  if (compact) return (((size_t)n.N * n.N * sizeof(double) + n.N * sizeof(unsigned short) + 7) / 8) * 8 * block;
   return ((size_t)n.N * (n.N + 1) + n.N) * block * sizeof(double);
 }
 
 // Compiles (or fetches from the per-process cache) the specialized kernel for
 // `n` and `block` threads per block on the current device.
-int gen_kernel(const DevNet &n, int block, void **fn_out, void **pro_out, std::string *err) {
+int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **pro_out, std::string *err) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaFree(0);  // make the device's primary context current for the driver API
-  const std::string src = generate_source(n, block);
+  const std::string src = generate_source(n, block, compact);
   const std::string key = std::to_string(dev) + ":" + std::to_string(block) + ":" + src;
   std::lock_guard<std::mutex> lock(g_cache_mutex);
   auto it = g_cache.find(key);
@@ -1073,16 +1144,16 @@ int gen_prep_fields(const DevNet &n) {
   return g.prep_fields();
 }
 
-int gen_blocks_per_sm(void *fn, const DevNet &n, int block) {
+int gen_blocks_per_sm(void *fn, const DevNet &n, int block, bool compact) {
   int nb = 0;
   const Driver &D = driver();
-  if (!D.ok || D.occupancy(&nb, (CUfunction)fn, block, gen_shared_bytes(n, block)) != CUDA_SUCCESS) return 0;
+  if (!D.ok || D.occupancy(&nb, (CUfunction)fn, block, gen_shared_bytes(n, block, compact)) != CUDA_SUCCESS) return 0;
   return nb;
 }
 
 // Prologue over all cells, then the persistent solve.
 cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, Scratch *scr, double *prep, int grid,
-                       int block, int refill, cudaStream_t st) {
+                       int block, int refill, cudaStream_t st, bool compact) {
   CellArgs args = a;
   double inv_dt = 1.0 / a.dt;
   const Driver &D = driver();
@@ -1092,7 +1163,7 @@ cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, 
   CUresult r = D.launchKernel((CUfunction)pro, pgrid, 1, 1, 128, 1, 1, 0, (CUstream)st, pparams, nullptr);
   if (r != CUDA_SUCCESS) return cudaErrorLaunchFailure;
   void *params[] = {&args, &scr, &refill, &inv_dt, &prep};
-  r = D.launchKernel((CUfunction)fn, grid, 1, 1, block, 1, 1, (unsigned)gen_shared_bytes(n, block), (CUstream)st,
+  r = D.launchKernel((CUfunction)fn, grid, 1, 1, block, 1, 1, (unsigned)gen_shared_bytes(n, block, compact), (CUstream)st,
                      params, nullptr);
   return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorLaunchFailure;
 }

@@ -234,7 +234,25 @@ def test_generic_table_driven_kernel(oracle, kind):
 def test_specialized_kernel_is_default():
     net, opt, cells, dt = workloads.calcite_cells(16, seed=14)
     step = ReactionStep(net, opt)
-    assert step.launch().variant == abi.KERNEL_SPECIALIZED
+    assert step.launch().variant in (abi.KERNEL_SPECIALIZED, abi.KERNEL_SPECIALIZED_COMPACT)
+
+
+@pytest.mark.parametrize("jac", [abi.JACOBIAN_REFERENCE, abi.JACOBIAN_EXACT])
+def test_compact_layout_equals_augmented_layout(jac):
+    """The compact shared-memory layout (right-hand side in registers) does
+    the same operations in the same order: bit-identical results."""
+    net, opt, cells, dt = workloads.synthetic_cells(8192, seed=61)
+    opt.jacobian = jac
+    out = {}
+    for variant in (abi.KERNEL_SPECIALIZED, abi.KERNEL_SPECIALIZED_COMPACT):
+        step = ReactionStep(net, opt)
+        step.set_launch(32, 1, 8, variant=variant)
+        d = cells.to_device()
+        step.react(d, dt)
+        out[variant] = d.to_host()
+    a, b = out[abi.KERNEL_SPECIALIZED], out[abi.KERNEL_SPECIALIZED_COMPACT]
+    for f in ("pri_molal", "total_out", "mnrl_rate", "mnrl_volfrac", "total_sorb_eq", "iterations", "status"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)
 
 
 @pytest.mark.parametrize("variant", [abi.KERNEL_SPECIALIZED, abi.KERNEL_GENERIC])
