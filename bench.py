@@ -38,8 +38,8 @@ METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start v
 UNIT = "cell solves/s"
 NCELLS = 2_097_152
 # DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
-# on 131,072 cells of the same workload (154.0 MB read + 51.1 MB written)
-TRAFFIC_BYTES_PER_CELL = (154023168 + 51135488) / 131072
+# on 524,288 cells of the same workload (560.6 MB read + 289.2 MB written)
+TRAFFIC_BYTES_PER_CELL = (560573696 + 289235456) / 524288
 
 
 def parse():
@@ -394,8 +394,8 @@ def main():
                      "frac": achieved_tflops / probe if probe else None,
                      "traffic": TRAFFIC_BYTES_PER_CELL * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pfchem_gen_react "
-                                       "launch on 131072 cells, scaled by cells "
-                                       "(profiles/pfchem_gen_react_synthetic12_131k.md)",
+                                       "launch on 524288 cells, scaled by cells "
+                                       "(profiles/pfchem_gen_react_synthetic12_524k.md)",
                      "peak_source": "measured DFMA throughput on this GPU (pfchem_probe_fp64_peak, FMA = 2 flops)",
                      "flops_per_step": flops,
                      "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
