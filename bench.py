@@ -389,7 +389,9 @@ def main():
         "mean_newton_iterations": mean_iters, "converged_cells": conv,
         "lane_efficiency": eff, "queue_drain_ms": drain,
         "iteration_histogram": np.bincount(g.iterations).tolist(),
-        "gpu_launches": args.steps * (1 if warm is None else 2 + 6 * ((n + 262143) // 262144)),
+        # per step: prologue + persistent solve; the warm start adds the weight
+        # packing (one launch per layer) and the fused MLP inference
+        "gpu_launches": args.steps * (2 if warm is None else 2 + 4 + 1),
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": probe, "unit": "TFLOP/s",
                      "frac": achieved_tflops / probe if probe else None,
                      "traffic": TRAFFIC_BYTES_PER_CELL * n,
