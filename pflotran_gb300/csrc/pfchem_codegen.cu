@@ -321,14 +321,27 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       o << "  L.P[" << j << "] = L.m[" << j << "]; double aP" << j << " = L.m[" << j << "];\n";
       if (sorb()) o << "  L.Sg[" << j << "] = 0.0; double aS" << j << " = 0.0;\n";
     }
+    // Jacobian entries touched by some complex: accumulated in registers and
+    // stored once (the same additions in the same complex order as a
+    // read-modify-write per contribution); the others are stored here
+    std::vector<std::vector<int>> contrib((size_t)N * N);
+    for (int i = 0; i < n.Nc; ++i)
+      for (int k = 0; k < n.cn[i]; ++k)
+        for (int l = 0; l < n.cn[i]; ++l) contrib[(size_t)n.cid[i][l] * N + n.cid[i][k]].push_back(i);
     if (jac)
       for (int i = 0; i < N; ++i)
         for (int k = 0; k < N; ++k)
-          o << "  " << J(i, k) << " = " << (i == k ? "L.m[" + I(i) + "] * L.jac_aq" : "0.0") << ";\n";
+          if (contrib[(size_t)i * N + k].empty())
+            o << "  " << J(i, k) << " = " << (i == k ? "L.m[" + I(i) + "] * L.jac_aq" : "0.0") << ";\n";
     // aqueous complexes (RTotal)
     // secondary-species part of the ionic strength (the primary part is added
     // where the ionic strength is used, at the then current molalities)
     o << "  double Iacc = 0.0, Csum = 0.0;\n";
+    if (jac && n.Nc > 0) {
+      o << "  double cj0";
+      for (int i = 1; i < n.Nc; ++i) o << ", cj" << i;
+      o << ";\n";
+    }
     for (int i = 0; i < n.Nc; ++i) {
       if (prod_cplx()) {
         int8_t ids[PFCHEM_MAX_NNZ];
@@ -350,18 +363,29 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         acc(o, "L.P[" + I(j) + "]", n.cnu[i][k], "c");
         acc(o, "aP" + I(j), std::fabs(n.cnu[i][k]), "c");
       }
-      if (jac) {
-        o << "    const double cj = c * L.jac_aq;\n";
-        for (int k = 0; k < n.cn[i]; ++k) {
-          const int j = n.cid[i][k];
-          o << "    { const double t = " << times(n.cnu[i][k], "cj") << ";\n";
-          for (int l = 0; l < n.cn[i]; ++l) acc(o, J(n.cid[i][l], j), n.cnu[i][l], "t");
-          o << "    }\n";
-        }
-      }
+      if (jac) o << "    cj" << i << " = c * L.jac_aq;\n";
       o << "  }\n";
     }
     o << "  L.Iacc = 0.5 * Iacc; L.Csum = Csum;\n";
+    if (jac) {
+      for (int l = 0; l < N; ++l)
+        for (int k = 0; k < N; ++k) {
+          const auto &cs = contrib[(size_t)l * N + k];
+          if (cs.empty()) continue;
+          o << "  { double v = " << (l == k ? "L.m[" + I(l) + "] * L.jac_aq" : "0.0") << ";\n";
+          for (int i : cs) {
+            double nuk = 0.0, nul = 0.0;
+            for (int q = 0; q < n.cn[i]; ++q) {
+              if (n.cid[i][q] == k) nuk = n.cnu[i][q];
+              if (n.cid[i][q] == l) nul = n.cnu[i][q];
+            }
+            o << "    { const double t = " << times(nuk, "cj" + I(i)) << ";";
+            acc(o, "v", nul, "t");
+            o << "    }\n";
+          }
+          o << "    " << J(l, k) << " = v; }\n";
+        }
+    }
     // ion exchange (RTotalSorbEqIonx)
     for (int r = 0; r < n.Nix; ++r) {
       const int nz = n.xn[r];
