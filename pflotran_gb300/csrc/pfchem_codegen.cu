@@ -789,9 +789,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     for (int j = 0; j < N; ++j) {
       if (n.use_log) {
         o << "  { const double u = copysign(fmin(fabs(x[" << j << "]), " << lit(n.max_dlnC) << "), x[" << j << "]);\n";
-        // inline: the only exponentials left in a product-form iteration
-        o << "    x[" << j << "] = u; const double e = " << (prod_any() ? "exp" : "xexp") << "(-u); mnew[" << j
-          << "] = L.m[" << j << "] * e;\n";
+        o << "    x[" << j << "] = u; const double e = xexp(-u); mnew[" << j << "] = L.m[" << j << "] * e;\n";
         if (n.rel_change_tol > 0.0) o << "    mrc = fmax(mrc, fabs(e - 1.0));\n";
         o << "    if (!(fabs(mnew[" << j << "]) <= 1.7976931348623157e308)) nf = true; }\n";
       }

