@@ -937,26 +937,26 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
     for (int j = 0; j < N; ++j) c.pri_act_coef[j] = 1;
     for (int i = 0; i < w.Nc; ++i) c.sec_act_coef[i] = 1;
   }
-  // two starting guesses: the residual norm at the previous-step guess now;
-  // Newton then starts from `alt` and keeps it if its first residual norm
-  // is no larger, else starts over from the previous-step guess with the
-  // ion-exchange warm start of that guess's evaluation
-  bool pending = false;
-  R rplain = R(DBL_MAX), srf0[SR];
-  Cell<R> plain;
   if (alt) {
-    for (int r = 0; r < w.Nsr; ++r) srf0[r] = c.srfcplxrxn_free_site_conc[r];
+    R srf[SR];
+    for (int r = 0; r < w.Nsr; ++r) srf[r] = c.srfcplxrxn_free_site_conc[r];
+    R rplain, ralt = R(DBL_MAX);
     residual_norm(w, o, c, fixed_accum, psv_t, dt, accum_scale, &rplain);  // inner status not used here
-    plain = c;
+    const Cell<R> plain = c;
     bool ok = true;
-    for (int j = 0; j < N; ++j)
-      if (!(alt[j] > 0.0 && alt[j] <= DBL_MAX)) ok = false;
-    if (ok) {
-      for (int j = 0; j < N; ++j) c.pri_molal[j] = R(alt[j]);
-      pending = true;
+    for (int j = 0; j < N; ++j) {
+      const double g = alt[j];
+      if (g > 0.0 && g <= DBL_MAX) c.pri_molal[j] = R(g);
+      else ok = false;
     }
-    for (int r = 0; r < w.Nsr; ++r) c.srfcplxrxn_free_site_conc[r] = srf0[r];
-    if (alt_used) *alt_used = false;
+    if (ok) {
+      R r;
+      if (residual_norm(w, o, c, fixed_accum, psv_t, dt, accum_scale, &r) && r < R(DBL_MAX)) ralt = r;
+    }
+    const bool take = ralt <= rplain;
+    if (!take) c = plain;
+    for (int r = 0; r < w.Nsr; ++r) c.srfcplxrxn_free_site_conc[r] = srf[r];
+    if (alt_used) *alt_used = take;
   }
   int status = PFCHEM_CELL_CONVERGED;
   R residual[P], J[P][P], update[P], prev_solution[P], new_solution[P];
@@ -968,34 +968,7 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
         break;
       }
     }
-    const int inner = newton_system(w, o, c, fixed_accum, psv_t, dt, residual, J);
-    if (pending) {
-      pending = false;
-      R ralt = R(DBL_MAX);
-      bool finite = true;
-      for (int j = 0; j < N; ++j)
-        if (!std::isfinite((double)residual[j])) finite = false;
-      if (!inner && finite) {
-        R r = 0;
-        if (o.residual_tol_kind == PFCHEM_RESIDUAL_RELATIVE) {
-          R S[P];
-          residual_scale(w, o, c, fixed_accum, psv_t, accum_scale, S);
-          for (int j = 0; j < N; ++j) r = std::max(r, std::fabs(residual[j]) / S[j]);
-        } else {
-          for (int j = 0; j < N; ++j) r = std::max(r, std::fabs(residual[j]));
-        }
-        ralt = r;
-      }
-      if (ralt <= rplain) {
-        if (alt_used) *alt_used = true;
-      } else {
-        c = plain;
-        for (int r = 0; r < w.Nsr; ++r) c.srfcplxrxn_free_site_conc[r] = srf0[r];
-        num_iterations = 0;
-        continue;
-      }
-    }
-    if (inner) {
+    if (newton_system(w, o, c, fixed_accum, psv_t, dt, residual, J)) {
       status = PFCHEM_CELL_INNER_MAXITER;
       break;
     }

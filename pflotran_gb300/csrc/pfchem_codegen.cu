@@ -285,7 +285,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         for (int q = 0; q < n.srn[r]; ++q)
           o << "  L.bs[" << (int)n.src[r][q] << "] = xexp(L.bs[" << (int)n.src[r][q] << "]);\n";
     o << "  L.Iacc = 0.0; L.Csum = 0.0;\n";
-    o << "  L.iter = 0; L.alt_pending = false; L.alt_used = false; L.rplain = 0.0;\n}\n";
+    o << "  L.iter = 0; L.alt_pending = false; L.alt_used = false;\n}\n";
   }
 
   // Residual (and with jac the Jacobian d/dln m into [J | .]) at L.m
@@ -755,7 +755,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   void newton_step() {
     const int N = n.N;
     o << "__device__ __forceinline__ int newton_step(Lane &L, double *Jb, " << (compact ? "unsigned short" : "long long")
-      << " *Eb, const CellArgs &a, long long cell, const double *prep) {\n";
+      << " *Eb) {\n";
     o << "  L.iter += 1;\n";
     if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) {
       o << "  if (L.iter > 1) {\n  double Iv = L.Iacc;\n";
@@ -764,22 +764,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       activity("Iv");
       o << "  }\n";
     }
-    o << "  int st = evaluate_jac(L, Jb);\n";
+    o << "  int st = evaluate_jac(L, Jb); if (st) return st;\n";
     o << "  bool bad; const bool conv = converged(L, &bad);\n";
-    // first evaluation at the alternative guess: keep it if its residual
-    // norm is no larger than the previous-step guess's, else start over
-    // from that guess and the ion-exchange warm start evaluated there
-    o << "  if (L.alt_pending) {\n    L.alt_pending = false;\n";
-    o << "    const double ralt = (st == 0 && !bad) ? rnorm(L) : 1.7976931348623157e308;\n";
-    o << "    if (ralt <= L.rplain) L.alt_used = true;\n    else {\n";
-    o << "      const long long nc = a.ncells;\n";
-    for (int j = 0; j < N; ++j)
-      o << "      L.m[" << j << "] = a.pri_molal[" << j << " * nc + cell]; L.lm[" << j << "] = xlog(L.m[" << j << "]);\n";
-    for (int r = 0; r < n.Nix; ++r)
-      o << "      L.ixr[" << r << "] = prep[" << ixr_field() + r << " * nc + cell];\n";
-    for (int r = 0; r < n.Nsr; ++r) o << "      L.srf[" << r << "] = a.srfree[" << r << " * nc + cell];\n";
-    o << "      L.iter = 0;\n      return -1;\n    }\n  }\n";
-    o << "  if (st) return st;\n";
     o << "  if (bad) return " << PFCHEM_CELL_NONFINITE << ";\n";
     o << "  if (conv) return " << PFCHEM_CELL_CONVERGED << ";\n";
     o << "  if (L.iter >= " << n.max_iter << ") return " << PFCHEM_CELL_MAXITER << ";\n";
@@ -885,10 +871,9 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   // guess, ln gamma and gamma of the primaries, the fixed accumulation, the
   // complex/mineral/surface constants, the ion-exchange warm starts, and
   // whether the alternative guess was taken.
-  int prep_fields() const { return ixr_field() + n.Nix + 2; }
-  // record field of the first ion-exchange warm start
-  int ixr_field() const {
-    return 5 * n.N + n.Nc + (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? n.Nc : 0) + 2 * n.Nm + n.Nsc;
+  int prep_fields() const {
+    return 5 * n.N + n.Nc + (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? n.Nc : 0) + 2 * n.Nm + n.Nsc +
+           n.Nix + 1;
   }
   void prep_io(bool store) {
     int f = 0;
@@ -909,13 +894,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     for (int k = 0; k < n.Nm; ++k) fld("L.rk[" + I(k) + "]");
     for (int k = 0; k < n.Nsc; ++k) fld("L.bs[" + I(k) + "]");
     for (int r = 0; r < n.Nix; ++r) fld("L.ixr[" + I(r) + "]");
-    if (store) {
-      o << "  prep[" << f << " * nc + cell] = L.alt_pending ? 1.0 : 0.0;\n";
-      o << "  prep[" << f + 1 << " * nc + cell] = L.rplain;\n";
-    } else {
-      o << "  L.alt_pending = prep[" << f << " * nc + cell] != 0.0;\n";
-      o << "  L.rplain = prep[" << f + 1 << " * nc + cell];\n";
-    }
+    if (store) o << "  prep[" << f << " * nc + cell] = L.alt_used ? 1.0 : 0.0;\n";
+    else o << "  L.alt_used = prep[" << f << " * nc + cell] != 0.0;\n";
   }
 
   // Data-parallel prologue: one thread per cell, every lane busy.  It does
@@ -926,23 +906,29 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     o << "extern \"C\" __global__ void __launch_bounds__(128) pfchem_gen_prologue(const __grid_constant__ CellArgs a, "
          "double *prep, double inv_dt, Scratch *scr) {\n";
     o << "  const long long cell = blockIdx.x * (long long)blockDim.x + threadIdx.x;\n";
-    o << "  const long long nc = a.ncells;\n";
+    o << "  const long long nc = a.ncells;\n  bool used = false;\n";
     o << "  if (cell < nc && !(a.active && a.active[cell] <= 0)) {\n";
     o << "  Lane L;\n  setup(L, a, cell, inv_dt);\n";
-    // the residual at the previous-step guess here; the one at the
-    // alternative guess is the solve kernel's first evaluation, which
-    // keeps the alternative where its norm is no larger
     o << "  if (a.alt_guess) {\n";
     o << "    evaluate_res(L, nullptr); bool bad; converged(L, &bad);\n";
-    o << "    L.rplain = bad ? 1.7976931348623157e308 : rnorm(L);\n";
-    o << "    bool ok = true; double g[NP];\n";
+    o << "    const double rplain = bad ? 1.7976931348623157e308 : rnorm(L);\n";
+    o << "    double pm[NP], plm[NP], pix[NIX];\n";
+    o << "    for (int j = 0; j < NP; ++j) { pm[j] = L.m[j]; plm[j] = L.lm[j]; }\n";
+    o << "    for (int r = 0; r < NIX; ++r) pix[r] = L.ixr[r];\n";
+    o << "    bool ok = true;\n";
     for (int j = 0; j < n.N; ++j)
-      o << "    g[" << j << "] = a.alt_guess[" << j << " * nc + cell]; if (!(g[" << j << "] > 0.0 && g[" << j
-        << "] <= 1.7976931348623157e308)) ok = false;\n";
-    o << "    if (ok) { for (int j = 0; j < NP; ++j) { L.m[j] = g[j]; L.lm[j] = xlog(g[j]); } L.alt_pending = true; }\n";
+      o << "    { const double g = a.alt_guess[" << j << " * nc + cell]; if (g > 0.0 && g <= 1.7976931348623157e308) { L.m["
+        << j << "] = g; L.lm[" << j << "] = xlog(g); } else ok = false; }\n";
+    o << "    double ralt = 1.7976931348623157e308;\n";
+    o << "    if (ok) { const int st = evaluate_res(L, nullptr); converged(L, &bad); if (!bad && st == 0) ralt = rnorm(L); }\n";
+    o << "    if (ralt <= rplain) { L.alt_used = true; used = true; }\n";
+    o << "    else { for (int j = 0; j < NP; ++j) { L.m[j] = pm[j]; L.lm[j] = plm[j]; } for (int r = 0; r < NIX; ++r) L.ixr[r] = pix[r]; }\n";
     o << "  }\n";
     prep_io(true);
-    o << "  }\n  (void)scr;\n}\n";
+    o << "  }\n";
+    o << "  const unsigned bal = __ballot_sync(0xffffffffu, used);\n";
+    o << "  if ((threadIdx.x & 31) == 0 && bal) atomicAdd(&scr->alt_used, (unsigned long long)__popc(bal));\n";
+    o << "}\n";
   }
 
   // The solve kernel's per-cell start: the prologue's record plus the
@@ -963,7 +949,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     for (int r = 0; r < n.Nsr; ++r) o << "  L.srf[" << r << "] = a.srfree[" << r << " * nc + cell];\n";
     prep_io(false);
     o << "  L.Icell = a.ionic[cell]; L.Iacc = 0.0; L.Csum = 0.0;\n";
-    o << "  L.iter = 0; L.alt_used = false;\n}\n";
+    o << "  L.iter = 0; L.alt_pending = false;\n}\n";
   }
 
   void kernel() {
@@ -1015,10 +1001,9 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     }
     ++my_trips;
     if (cell >= 0) {
-      int st = newton_step(L, Jb, Eb, a, cell, prep);
+      int st = newton_step(L, Jb, Eb);
       if (st >= 0) {
         finalize(L, a, cell, st);
-        my_alt += L.alt_used ? 1 : 0;
         my_iters += L.iter;
         my_max = max(my_max, (unsigned)L.iter);
         if (st != 0) my_bad += 1;
@@ -1036,7 +1021,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     atomicAdd(&scr->sum_iter, my_iters);
     atomicAdd(&scr->newton_trips, my_trips);
     atomicMax(&scr->t_end, pf_now());
-    atomicAdd(&scr->alt_used, my_alt);
+    (void)my_alt;
     atomicMax(&scr->max_iter, my_max);
     atomicAdd(&scr->nonconverged, my_bad);
   }
