@@ -187,7 +187,7 @@ class OperatorSplitRun:
 
     def __init__(self, shape=(128, 128, 128), dt=86400.0, sigma=1.5, corr_len=10.0, seed=11, warm_start=True,
                  train_samples=2_097_152, epochs=8, autotune=True, drift_sample=512,
-                 cells_per_step=2.0, courant=0.9, device="cuda", log=print):
+                 cells_per_step=2.0, courant=0.9, device="cuda", log=print, jacobian=0):
         import torch
         from . import workloads
         from .lib import ReactionStep
@@ -203,6 +203,7 @@ class OperatorSplitRun:
         net = workloads.synthetic_network()
         self.net = net
         _, self.opt, cells, _ = workloads.synthetic_cells(n, seed=seed, net=net, device=device)
+        self.opt.jacobian = jacobian  # PFCHEM_JACOBIAN_*
         cells.sec_molal = np.zeros(max(net.Nc, 1) * n)
         d = cells.to_device(device)
         d.total_out.copy_(d.total)  # transport reads the previous step's aqueous totals

@@ -52,7 +52,8 @@ def test_timestepped_full_size(oracle):
     solves/s, iteration histograms and drift (report to the path in
     PFCHEM_TIMESTEPPED_FULL)."""
     from pflotran_gb300.os_run import OperatorSplitRun
-    run = OperatorSplitRun(shape=(128, 128, 128), warm_start=True, autotune=True, drift_sample=512)
+    jac = 1 if os.environ.get("PFCHEM_TIMESTEPPED_JACOBIAN") == "exact" else 0
+    run = OperatorSplitRun(shape=(128, 128, 128), warm_start=True, autotune=True, drift_sample=512, jacobian=jac)
     recs = run.run(steps=50, oracle_fn=_oracle_fn(oracle))
     with open(os.environ["PFCHEM_TIMESTEPPED_FULL"], "w") as f:
         json.dump({"setup": run.report, "steps": recs}, f)
