@@ -1,6 +1,8 @@
-"""Builds the in-tree CUDA library libpfchem.so for sm_103a with nvcc.
+"""Builds the in-tree CUDA libraries for sm_103a with nvcc: libpfchem.so
+(the chemistry library), libpfchem_probe.so (the FP64 peak probe) and
+libpfchem_transport.so (the time-stepped run's upwind transport).
 
-Two translation units compiled in parallel, then linked; output in
+Translation units compiled in parallel, then linked; output in
 pflotran_gb300/_build/.  Re-running skips the build when no source changed.
 """
 import hashlib
@@ -16,6 +18,8 @@ LIB = os.path.join(OUT, "libpfchem.so")
 PROBE = os.path.join(OUT, "libpfchem_probe.so")
 SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu", "pfchem_codegen.cu", "pfchem_mlp.cu"]
 PROBE_SOURCES = ["fp64_peak.cu"]
+TRANSPORT = os.path.join(OUT, "libpfchem_transport.so")
+TRANSPORT_SOURCES = ["transport_upwind.cu"]
 HEADERS = ["pfchem_device.cuh", os.path.join("..", "..", "include", "pfchem.h")]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-lineinfo", "-std=c++17",
               "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -34,7 +38,7 @@ def _cuda_home():
 
 def _digest():
     h = hashlib.sha256()
-    for f in SOURCES + PROBE_SOURCES + HEADERS:
+    for f in SOURCES + PROBE_SOURCES + TRANSPORT_SOURCES + HEADERS:
         with open(os.path.join(CSRC, f), "rb") as fh:
             h.update(fh.read())
     h.update(" ".join(NVCC_FLAGS).encode())
@@ -45,7 +49,8 @@ def build(force=False, verbose=False):
     os.makedirs(OUT, exist_ok=True)
     stamp = os.path.join(OUT, "stamp")
     dig = _digest()
-    if (not force and os.path.exists(LIB) and os.path.exists(PROBE) and os.path.exists(stamp)
+    if (not force and os.path.exists(LIB) and os.path.exists(PROBE) and os.path.exists(TRANSPORT)
+            and os.path.exists(stamp)
             and open(stamp).read() == dig):
         return LIB
     nvcc = _nvcc()
@@ -60,9 +65,11 @@ def build(force=False, verbose=False):
             sys.stderr.write(r.stderr)
         return obj
 
-    with ThreadPoolExecutor(len(SOURCES) + len(PROBE_SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES + PROBE_SOURCES))
-    for target, o in ((LIB, objs[:len(SOURCES)]), (PROBE, objs[len(SOURCES):])):
+    all_src = SOURCES + PROBE_SOURCES + TRANSPORT_SOURCES
+    with ThreadPoolExecutor(len(all_src)) as ex:
+        objs = list(ex.map(compile_one, all_src))
+    a, b = len(SOURCES), len(SOURCES) + len(PROBE_SOURCES)
+    for target, o in ((LIB, objs[:a]), (PROBE, objs[a:b]), (TRANSPORT, objs[b:])):
         tmp = target + ".tmp"
         cmd = [nvcc, "-shared", "-gencode", "arch=compute_103a,code=sm_103a", "-o", tmp] + o
         if target == LIB:

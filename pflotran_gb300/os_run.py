@@ -21,10 +21,13 @@ structured grid of unit cells, entirely on one GPU:
 * the reaction step (`ReactionStep.react_async`, learned warm start
   optional) over every cell.
 
-Transport (torch tensor ops), a gather of the sampled cells' pre-step state
-for the drift check and the reaction step are captured into ONE CUDA graph,
-replayed once per step.  Transport is harness code: the library's boundary
-is the reaction step, as RTReact's is.
+Transport (one CUDA kernel per sub-step from libpfchem_transport.so on
+precomputed per-cell upwind weights, or the flux form as torch tensor ops
+with transport="torch"), a gather of the
+sampled cells' pre-step state for the drift check and the reaction step are
+captured into ONE CUDA graph, replayed once per step.  Transport is not part
+of the chemistry library: the library's boundary is the reaction step, as
+RTReact's is.
 """
 from __future__ import annotations
 
@@ -153,6 +156,67 @@ def upwind_advect(T, qx, qy, qz, pore_vol, dt_sub, inflow):
     return T + (dt_sub / pore_vol) * div
 
 
+_transport_lib = None
+
+
+def _transport():
+    """libpfchem_transport.so (built with the chemistry library)."""
+    global _transport_lib
+    if _transport_lib is None:
+        import ctypes as C
+        import os
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libpfchem_transport.so")
+        if not os.path.exists(path):
+            from .build import build
+            build()
+        lib = C.CDLL(path)
+        vp = C.c_void_p
+        lib.pfchem_transport_upwind.argtypes = [vp] * 5 + [C.c_int] * 5 + [vp]
+        lib.pfchem_transport_upwind.restype = C.c_int
+        _transport_lib = lib
+    return _transport_lib
+
+
+def upwind_coefficients(qx, qy, qz, pore_vol, dt_sub):
+    """Per-cell weights [7, nx, ny, nz] of one `upwind_advect` sub-step
+    written as T' = a0 T + sum_f a_f T_f over the six neighbours f = west,
+    east, south, north, bottom, top: a0 = 1 - s * (outgoing flux), a_f =
+    s * (incoming flux through f) (0 where f is an outlet or closed), s =
+    dt_sub / pore_vol.  The west weight of an x = 0 cell multiplies the
+    inflow composition."""
+    import torch
+    s = dt_sub / pore_vol
+    pos = lambda q: q.clamp(min=0.0)
+    a = torch.stack([1.0 - s * outflow_rate(qx, qy, qz),
+                     s * pos(qx[:-1]), s * pos(-qx[1:]),
+                     s * pos(qy[:, :-1]), s * pos(-qy[:, 1:]),
+                     s * pos(qz[:, :, :-1]), s * pos(-qz[:, :, 1:])])
+    a[2, -1] = 0.0       # nothing enters through the east outlet
+    a[3, :, 0] = 0.0     # closed y and z boundaries
+    a[4, :, -1] = 0.0
+    a[5, :, :, 0] = 0.0
+    a[6, :, :, -1] = 0.0
+    return a.contiguous()
+
+
+def upwind_advect_cuda(T0, T1, tmp, coef, inflow, nsub, stream):
+    """`nsub` sub-steps of `upwind_advect` (weights from
+    `upwind_coefficients`) in one CUDA kernel each, from T0 into T1 (tmp:
+    scratch like T1), enqueued on `stream`.  The same update as
+    `upwind_advect` up to rounding (the weights are summed in another
+    order)."""
+    for t in (T0, T1, tmp, coef, inflow):
+        if not (t.is_cuda and t.is_contiguous() and t.dtype == T0.dtype):
+            raise ValueError("upwind_advect_cuda: contiguous float64 CUDA tensors expected")
+    ncomp, nx, ny, nz = T0.shape
+    if tuple(coef.shape) != (7, nx, ny, nz) or tuple(inflow.shape) != (ncomp,):
+        raise ValueError("upwind_advect_cuda: coef [7, nx, ny, nz] and inflow [ncomp] expected")
+    err = _transport().pfchem_transport_upwind(T0.data_ptr(), T1.data_ptr(), tmp.data_ptr(), coef.data_ptr(),
+                                               inflow.data_ptr(), ncomp, nx, ny, nz, nsub, stream.cuda_stream)
+    if err != 0:
+        raise RuntimeError(f"pfchem_transport_upwind: CUDA error {err}")
+
+
 def drift(net, gpu, ref, mask):
     """Max scaled relative differences GPU vs oracle over the `mask` cells:
     free-ion molalities (relative), aqueous totals (scaled by the sum of the
@@ -187,7 +251,7 @@ class OperatorSplitRun:
 
     def __init__(self, shape=(128, 128, 128), dt=86400.0, sigma=1.5, corr_len=10.0, seed=11, warm_start=True,
                  train_samples=2_097_152, epochs=8, autotune=True, drift_sample=512,
-                 cells_per_step=2.0, courant=0.9, device="cuda", log=print, jacobian=0):
+                 cells_per_step=2.0, courant=0.9, device="cuda", log=print, jacobian=0, transport="cuda"):
         import torch
         from . import workloads
         from .lib import ReactionStep
@@ -200,6 +264,9 @@ class OperatorSplitRun:
         self.seed = seed
         self.drift_sample = min(int(drift_sample), n)
         self.device = device
+        if transport not in ("cuda", "torch"):
+            raise ValueError(f"transport: 'cuda' or 'torch', not {transport!r}")
+        self.transport = transport
         net = workloads.synthetic_network()
         self.net = net
         _, self.opt, cells, _ = workloads.synthetic_cells(n, seed=seed, net=net, device=device)
@@ -243,10 +310,15 @@ class OperatorSplitRun:
         self.nsub = max(1, int(math.ceil(dt * out_max / self.pore_vol / courant)))
         torch.cuda.synchronize()
         self.report["flow"] = {"cg_iterations": cg_its, "s": time.perf_counter() - t0, "substeps": self.nsub,
+                               "transport": transport,
                                "lnK_std": float(torch.log(K).std()), "max_cell_courant": dt * out_max / self.pore_vol}
         # inflow water: the equilibrium totals of one cell of the same distribution
         _, _, w, _ = workloads.synthetic_cells(1, seed=seed + 7, net=net, device=device)
         self.inflow = torch.as_tensor(w.total, device=device)
+        self.tmp = self.coef = None
+        if transport == "cuda":
+            self.tmp = torch.empty_like(d.total)
+            self.coef = upwind_coefficients(self.qx, self.qy, self.qz, self.pore_vol, dt / self.nsub)
         # sampled cells for the drift check (indices refreshed before each replay)
         self.idx = torch.zeros(self.drift_sample, dtype=torch.long, device=device)
         self.snap = {f: torch.empty((getattr(d, f).numel() // n, self.drift_sample), dtype=torch.float64,
@@ -258,10 +330,15 @@ class OperatorSplitRun:
         import torch
         d = self.cells
         N = self.net.N
-        T = d.total_out.view(N, *self.shape)
-        for _ in range(self.nsub):
-            T = upwind_advect(T, self.qx, self.qy, self.qz, self.pore_vol, self.dt / self.nsub, self.inflow)
-        d.total.copy_(T.reshape(-1))
+        if self.transport == "cuda":
+            shp = (N,) + self.shape
+            upwind_advect_cuda(d.total_out.view(shp), d.total.view(shp), self.tmp.view(shp), self.coef, self.inflow,
+                               self.nsub, stream)
+        else:
+            T = d.total_out.view(N, *self.shape)
+            for _ in range(self.nsub):
+                T = upwind_advect(T, self.qx, self.qy, self.qz, self.pore_vol, self.dt / self.nsub, self.inflow)
+            d.total.copy_(T.reshape(-1))
         for f, buf in self.snap.items():
             a = getattr(d, f)
             torch.index_select(a.view(-1, self.n), 1, self.idx, out=buf)

@@ -56,3 +56,35 @@ def test_upwind_preserves_uniform_state_and_balances_mass():
         T = Tn
         assert float(T.min()) >= -1e-15 and float(T.max()) <= 1.0 + 1e-12  # monotone under CFL
     assert float(T[0, 0].mean()) > float(T[0, -1].mean())
+
+
+def test_transport_library_exports_the_upwind_step():
+    import ctypes
+    lib = os_run._transport()
+    assert isinstance(lib.pfchem_transport_upwind, ctypes._CFuncPtr)
+
+
+def test_upwind_weights_reproduce_the_flux_form():
+    """T' = a0 T + sum_f a_f T_f with the per-cell weights equals the flux
+    form to rounding; the weights are non-negative under the CFL limit and
+    sum (with the outflow) to one."""
+    K, qx, qy, qz, _ = _flow()
+    por = 0.25
+    dt = 0.9 * por / float(os_run.outflow_rate(qx, qy, qz).max())
+    a = os_run.upwind_coefficients(qx, qy, qz, por, dt)
+    assert a.shape == (7,) + K.shape
+    assert float(a.min()) >= 0.0
+    g = torch.Generator().manual_seed(2)
+    T = torch.rand((3,) + K.shape, dtype=torch.float64, generator=g)
+    inflow = torch.tensor([0.5, 2.0, 1.0], dtype=torch.float64)
+    nb = torch.zeros((6,) + T.shape, dtype=torch.float64)
+    nb[0, :, 1:] = T[:, :-1]
+    nb[0, :, 0] = inflow[:, None, None]
+    nb[1, :, :-1] = T[:, 1:]
+    nb[2, :, :, 1:] = T[:, :, :-1]
+    nb[3, :, :, :-1] = T[:, :, 1:]
+    nb[4, :, :, :, 1:] = T[:, :, :, :-1]
+    nb[5, :, :, :, :-1] = T[:, :, :, 1:]
+    out = a[0] * T + (a[1:, None] * nb).sum(0)
+    ref = os_run.upwind_advect(T, qx, qy, qz, por, dt, inflow)
+    assert float((out - ref).abs().max()) <= 1e-14 * float(ref.abs().max())
