@@ -78,3 +78,20 @@ def constraint_problem(oracle, net, opt, cells, rows):
         elif kind.startswith("mineral:"):
             types[j], minerals[j], values[j] = abi.CONSTRAINT_MINERAL, int(kind.split(":")[1]), molar[j]
     return types, minerals, np.ascontiguousarray(values)
+
+
+def error_statement(net, x, y, mask=None):
+    """Max and 99th percentile of the scaled relative errors of x against y
+    (cells in `mask`) for the aqueous totals, mineral volume fractions and
+    mineral rates, with the scales of `compare`."""
+    n = y.ncells
+    if mask is None:
+        mask = np.ones(n, bool)
+    errs = {"total": rel_err(x.total_out.reshape(net.N, n), y.total_out.reshape(net.N, n), total_scale(net, y))}
+    if net.Nm:
+        k = np.array([mn.extra["k"] for mn in net.minerals])[:, None]
+        area = y.mnrl_area.reshape(-1, n)[:net.Nm]
+        errs["mnrl_rate"] = rel_err(x.mnrl_rate.reshape(-1, n)[:net.Nm], y.mnrl_rate.reshape(-1, n)[:net.Nm], k * area)
+        errs["mnrl_volfrac"] = rel_err(x.mnrl_volfrac.reshape(-1, n)[:net.Nm], y.mnrl_volfrac.reshape(-1, n)[:net.Nm],
+                                       1e-300)
+    return {q: {"max": float(e[:, mask].max()), "p99": float(np.percentile(e[:, mask], 99))} for q, e in errs.items()}

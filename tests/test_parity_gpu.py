@@ -399,3 +399,46 @@ def test_large_host_batch_equals_device_batch(warm):
     assert st_host.sum_iterations == st_dev.sum_iterations
     assert st_host.nonconverged == st_dev.nonconverged
     assert st_host.alt_guess_used == st_dev.alt_guess_used
+
+
+@pytest.mark.parametrize("kind", ["calcite", "synthetic"])
+def test_error_statement_against_extended_precision(oracle, kind):
+    """GPU vs the double oracle (the parity bar) and both against the
+    oracle's long-double instantiation (binary128 on aarch64, 80-bit
+    extended on x86-64), max and 99th percentile, on totals, mineral volume
+    fractions and rates.  The extended-precision solve stops at the same
+    1e-12 relative residual, so its distance to either double solve is the
+    convergence tolerance times the cell's conditioning; the GPU must be no
+    further from it than the double oracle is, beyond that level.  The
+    report goes to the path in PFCHEM_ERROR_STATEMENT when it is set."""
+    import json
+    import os
+    if kind == "calcite":
+        net, opt, cells, dt = workloads.calcite_cells(4096, seed=21, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(2048, seed=21)
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    ext = cells.copy()
+    if ext.sec_molal is None:
+        ext.sec_molal = np.zeros(max(net.Nc, 1) * cells.ncells)
+    oracle.react(net.as_struct(), opt, dt, ext, 1, os.cpu_count() or 1)
+    ok = (ref.status == 0) & (gpu.status == 0) & (ext.status == 0)
+    assert ok.mean() > 0.99
+    from helpers import error_statement
+    rep = {"gpu_vs_double": error_statement(net, gpu, ref, ok),
+           "gpu_vs_extended": error_statement(net, gpu, ext, ok),
+           "double_vs_extended": error_statement(net, ref, ext, ok),
+           "cells": int(ok.sum()), "long_double_digits": int(np.finfo(np.longdouble).precision)}
+    print(kind, json.dumps(rep))
+    path = os.environ.get("PFCHEM_ERROR_STATEMENT")
+    if path:
+        old = json.load(open(path)) if os.path.exists(path) else {}
+        old[kind] = rep
+        with open(path, "w") as f:
+            json.dump(old, f, indent=1)
+    for q, e in rep["gpu_vs_double"].items():
+        assert e["max"] <= TOL, (q, e)
+    for q, e in rep["gpu_vs_extended"].items():
+        d = rep["double_vs_extended"][q]
+        assert e["max"] <= 1e-8, (q, e)
+        assert e["p99"] <= 4 * d["p99"] + 1e-12, (q, e, d)
