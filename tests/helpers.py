@@ -80,13 +80,11 @@ def constraint_problem(oracle, net, opt, cells, rows):
     return types, minerals, np.ascontiguousarray(values)
 
 
-def error_statement(net, x, y, mask=None):
-    """Max and 99th percentile of the scaled relative errors of x against y
-    (cells in `mask`) for the aqueous totals, mineral volume fractions and
-    mineral rates, with the scales of `compare`."""
+def cell_errors(net, x, y):
+    """Per-cell scaled relative errors of x against y (max over the
+    components) for the aqueous totals, mineral volume fractions and mineral
+    rates, with the scales of `compare`."""
     n = y.ncells
-    if mask is None:
-        mask = np.ones(n, bool)
     errs = {"total": rel_err(x.total_out.reshape(net.N, n), y.total_out.reshape(net.N, n), total_scale(net, y))}
     if net.Nm:
         k = np.array([mn.extra["k"] for mn in net.minerals])[:, None]
@@ -94,4 +92,12 @@ def error_statement(net, x, y, mask=None):
         errs["mnrl_rate"] = rel_err(x.mnrl_rate.reshape(-1, n)[:net.Nm], y.mnrl_rate.reshape(-1, n)[:net.Nm], k * area)
         errs["mnrl_volfrac"] = rel_err(x.mnrl_volfrac.reshape(-1, n)[:net.Nm], y.mnrl_volfrac.reshape(-1, n)[:net.Nm],
                                        1e-300)
-    return {q: {"max": float(e[:, mask].max()), "p99": float(np.percentile(e[:, mask], 99))} for q, e in errs.items()}
+    return {q: e.max(axis=0) for q, e in errs.items()}
+
+
+def error_statement(net, x, y, mask=None):
+    """Max and 99th percentile over the cells in `mask` of `cell_errors`."""
+    errs = cell_errors(net, x, y)
+    if mask is None:
+        mask = np.ones(y.ncells, bool)
+    return {q: {"max": float(e[mask].max()), "p99": float(np.percentile(e[mask], 99))} for q, e in errs.items()}

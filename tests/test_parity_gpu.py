@@ -408,9 +408,14 @@ def test_error_statement_against_extended_precision(oracle, kind):
     extended on x86-64), max and 99th percentile, on totals, mineral volume
     fractions and rates.  The extended-precision solve stops at the same
     1e-12 relative residual, so its distance to either double solve is the
-    convergence tolerance times the cell's conditioning; the GPU must be no
-    further from it than the double oracle is, beyond that level.  The
-    report goes to the path in PFCHEM_ERROR_STATEMENT when it is set."""
+    convergence tolerance times the cell's conditioning.  Bar, per cell and
+    quantity: within 1e-10 of the double oracle, or, on a cell where the
+    double oracle itself is further than 1e-10 from the extended-precision
+    solution (an ill-conditioned cell whose double Newton path the
+    platform's libm rounding moves), within 1e-10 of the latter; and the
+    GPU's p99 distance to the extended solution no worse than the double
+    oracle's beyond the 1e-12 level.  The report goes to the path in
+    PFCHEM_ERROR_STATEMENT when it is set."""
     import json
     import os
     if kind == "calcite":
@@ -424,10 +429,13 @@ def test_error_statement_against_extended_precision(oracle, kind):
     oracle.react(net.as_struct(), opt, dt, ext, 1, os.cpu_count() or 1)
     ok = (ref.status == 0) & (gpu.status == 0) & (ext.status == 0)
     assert ok.mean() > 0.99
-    from helpers import error_statement
+    from helpers import cell_errors, error_statement
+    gd, ge, de = cell_errors(net, gpu, ref), cell_errors(net, gpu, ext), cell_errors(net, ref, ext)
+    ill = {q: ok & (de[q] > TOL) for q in gd}
     rep = {"gpu_vs_double": error_statement(net, gpu, ref, ok),
            "gpu_vs_extended": error_statement(net, gpu, ext, ok),
            "double_vs_extended": error_statement(net, ref, ext, ok),
+           "double_further_than_bar_from_extended": {q: int(m.sum()) for q, m in ill.items()},
            "cells": int(ok.sum()), "long_double_digits": int(np.finfo(np.longdouble).precision)}
     print(kind, json.dumps(rep))
     path = os.environ.get("PFCHEM_ERROR_STATEMENT")
@@ -436,8 +444,9 @@ def test_error_statement_against_extended_precision(oracle, kind):
         old[kind] = rep
         with open(path, "w") as f:
             json.dump(old, f, indent=1)
-    for q, e in rep["gpu_vs_double"].items():
-        assert e["max"] <= TOL, (q, e)
+    for q in gd:
+        good = np.where(ill[q], ge[q] <= TOL, gd[q] <= TOL)
+        assert good[ok].all(), (q, rep)
     for q, e in rep["gpu_vs_extended"].items():
         d = rep["double_vs_extended"][q]
         assert e["max"] <= 1e-8, (q, e)
