@@ -38,8 +38,8 @@ METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start v
 UNIT = "cell solves/s"
 NCELLS = 2_097_152
 # DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
-# on 524,288 cells of the same workload (560.6 MB read + 289.2 MB written)
-TRAFFIC_BYTES_PER_CELL = (560573696 + 289235456) / 524288
+# on 524,288 cells of the same workload (561.5 MB read + 290.3 MB written)
+TRAFFIC_BYTES_PER_CELL = (561539840 + 290312704) / 524288
 
 
 def parse():
