@@ -1579,10 +1579,6 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
 }  // namespace
 
 extern "C" {
-// Constraint speciation of one cell given as a 1-cell batch (host pointers).
-// type[i]: 1 TOTAL [mol/L], 2 FREE [mol/L], 3 CHARGE_BAL (conc = guess).
-// Writes pri_molal, total_out, sec_molal, sorption state and the ionic
-// strength (at the final state, recomputed as the next LAG update would).
 // Constraint speciation of every cell of `cells` (host pointers): one
 // constraint row per component (types and mineral ids shared by the batch,
 // values per cell), `nthreads` std::threads.  Writes what the single-cell
@@ -1629,6 +1625,11 @@ int pfo_equilibrate_constraints(const pfchem_network *net, const pfchem_options 
   return bad.load();
 }
 
+// Constraint speciation of one cell given as a 1-cell batch (host pointers).
+// type[i]: 1 TOTAL [mol/L], 2 FREE [mol/L], 3 CHARGE_BAL (conc = guess),
+// 4 pH, 5 log10 FREE [mol/L] (no mineral rows: those need the batch entry).
+// Writes pri_molal, total_out, sec_molal, sorption state and the ionic
+// strength (at the final state, recomputed as the next LAG update would).
 int pfo_equilibrate_constraint(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
                                const int *type, const double *conc, int *iters) {
   Net w = make_net(net, opt);

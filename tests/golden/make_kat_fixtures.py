@@ -9,6 +9,10 @@ It reads, as text, the database rows and the regression gold values of
 
   regression_tests/ascem/batch/calcite-kinetics.{in,regression.gold} + calcite.dat
   regression_tests/ascem/batch/ion-exchange-valocchi.{in,regression.gold} + hanford.dat
+  regression_tests/ascem/batch/surface-complexation-1.{in,regression.gold}
+      + surface-complexation.dat
+  regression_tests/ascem/batch/{carbonate,ca-carbonate}-{unit,debye-huckel}-activity
+      .{in,regression.gold} + carbonate.dat / ca-carbonate.dat
 
 and records them with the deck parameters the tests need (cited per deck
 line below).  Nothing of PFLOTRAN is executed.
@@ -65,6 +69,14 @@ def parse_rxn(toks, ntemp, mineral=False):
     return out
 
 
+def parse_srfcplx(toks, ntemp):
+    # 'name' n (nu 'species') x n  logK x ntemp  Z molar_weight
+    nsp = int(toks[0])
+    st = [(toks[2 + 2 * k].strip("'"), float(toks[1 + 2 * k])) for k in range(nsp)]
+    i = 1 + 2 * nsp
+    return dict(stoich=st, logK=[float(x) for x in toks[i:i + ntemp]], Z=float(toks[i + ntemp]))
+
+
 def read_gold(path):
     gold = {}
     key = None
@@ -118,6 +130,50 @@ def main(root):
     )
     with open(os.path.join(HERE, "kat_ion_exchange_valocchi.json"), "w") as f:
         json.dump(fx, f, indent=1)
+    # --- surface-complexation-1 ---------------------------------------------
+    pri = ["H+", "Na+", "NO3-", "Zn++"]                                        # .in PRIMARY_SPECIES
+    sec = ["OH-", "Zn(OH)2(aq)", "Zn(OH)3-", "Zn(OH)4--", "ZnOH+"]              # .in SECONDARY_SPECIES
+    srf = [">FeOH2+_w", ">FeO-_w", ">FeOHZn+_w"]                               # .in COMPLEXES
+    temps, rows = read_dat(os.path.join(batch, "surface-complexation.dat"), set(pri + sec + srf))
+    fx = dict(
+        source="regression_tests/ascem/batch/surface-complexation-1.in + surface-complexation.dat "
+               "+ .regression.gold (time 0: the gold is the initial constraint state)",
+        temperatures=temps,
+        primaries=[dict(name=p, **parse_primary(rows[p])) for p in pri],
+        complexes=[dict(name=s, **parse_rxn(rows[s], len(temps))) for s in sec],
+        # SORPTION SURFACE_COMPLEXATION_RXN EQUILIBRIUM SITE >FeOH_w 7.6355e4 (mol/m^3 bulk)
+        surface=dict(site=">FeOH_w", site_density=7.6355e4,
+                     complexes=[dict(name=s, **parse_srfcplx(rows[s], len(temps))) for s in srf]),
+        porosity=0.9, volume=1.0,                                  # POROSITY 0.9d0; 1 m^3 cell
+        # CONSTRAINT initial: H+ 5.0 P, Na+ 1.0e-5 Z, NO3- 1.0e-1 T, Zn++ 1.0e-7 T
+        constraint=dict(types=[4, 3, 1, 1], conc=[5.0, 1e-5, 1e-1, 1e-7]),
+        log_formulation=True, act_coef="TIMESTEP",
+        gold=read_gold(os.path.join(batch, "surface-complexation-1.regression.gold")),
+    )
+    with open(os.path.join(HERE, "kat_surface_complexation_1.json"), "w") as f:
+        json.dump(fx, f, indent=1)
+    # --- carbonate speciation decks (all at time 0: the constraint state) ----
+    decks = {}
+    for deck, dat, pri, sec, conc in (
+            ("carbonate", "carbonate.dat", ["H+", "HCO3-"], ["OH-", "CO3--", "CO2(aq)"], [1e-3, 1e-3]),
+            ("ca-carbonate", "ca-carbonate.dat", ["HCO3-", "Ca++", "H+"],
+             ["OH-", "CO2(aq)", "CO3--", "CaOH+", "CaHCO3+", "CaCO3(aq)"], [3e-3, 1e-3, 1e-3])):
+        temps, rows = read_dat(os.path.join(batch, dat), set(pri + sec))
+        for act in ("unit", "debye-huckel"):
+            name = f"{deck}-{act}-activity"
+            decks[name] = dict(
+                source=f"regression_tests/ascem/batch/{name}.in + {dat} + .regression.gold (time 0)",
+                temperatures=temps,
+                primaries=[dict(name=p, **parse_primary(rows[p])) for p in pri],
+                complexes=[dict(name=s, **parse_rxn(rows[s], len(temps))) for s in sec],
+                porosity=0.25, volume=1.0,                      # POROSITY 0.25d0; 1 m^3 cell
+                constraint=dict(types=[1] * len(pri), conc=conc),  # CONSTRAINT initial: T rows
+                # ACTIVITY_COEFFICIENTS TIMESTEP in the debye-huckel decks, absent (off) in the others
+                log_formulation=True, act_coef="TIMESTEP" if act == "debye-huckel" else "OFF",
+                gold=read_gold(os.path.join(batch, f"{name}.regression.gold")),
+            )
+    with open(os.path.join(HERE, "kat_carbonate_speciation.json"), "w") as f:
+        json.dump(decks, f, indent=1)
 
 
 if __name__ == "__main__":

@@ -39,10 +39,15 @@ def build_network(fx, oracle):
     temps = fx["temperatures"]
     prim = [(p["name"], p["Z"], p["a0"]) for p in fx["primaries"]]
     net = ReactionNetwork(prim, debye=debye_25C())
+    def fit(logK):
+        # reaction_aux.F90:1336-1408; entries with log K at one temperature
+        # only (500 elsewhere) have no fit and keep their 25 C value
+        return tuple(oracle.fit_logK(temps, logK)) if sum(abs(k - 500.0) > 1e-10 for k in logK) >= 5 else None
+
     for c in fx.get("complexes", []):
         st = {s: v for s, v in c["stoich"] if s != "H2O"}
         h2o = sum(v for s, v in c["stoich"] if s == "H2O")
-        coef = tuple(oracle.fit_logK(temps, c["logK"]))  # reaction_aux.F90:1336-1408
+        coef = fit(c["logK"])
         # transport-only runs are isothermal (factory_subsurface.F90:368-374): log K is the
         # database value at the 25 C reference temperature (reaction_aux.F90:1412-1457)
         net.add_complex(c["name"], st, logK=c["logK"][temps.index(25.0)], Z=c["Z"], a0=c["a0"],
@@ -55,6 +60,14 @@ def build_network(fx, oracle):
                                 logKcoef=coef)
     if "ionx" in fx:
         net.add_ion_exchange([(c, k) for c, k in fx["ionx"]["cations"]], fx["ionx"]["CEC"])
+    if "surface" in fx:
+        sf = fx["surface"]
+        cx = []
+        for c in sf["complexes"]:
+            rest = {s: v for s, v in c["stoich"] if s != sf["site"] and s != "H2O"}
+            fs = sum(v for s, v in c["stoich"] if s == sf["site"])
+            cx.append((rest, fs, c["logK"][temps.index(25.0)]))
+        net.add_surface_complexation(sf["site_density"], cx)
     net.build()
     return net
 
@@ -72,6 +85,8 @@ def one_cell(net, fx, oracle):
         b.mnrl_area[:] = fx.get("area", 1.0)
     if net.Nix:
         b.eqionx_ref_cation_sorbed_conc[:] = 1e-9  # reactive_transport_aux.F90 initial value
+    if net.Nsr:
+        b.srfcplxrxn_free_site_conc[:] = 1e-9      # likewise
     return b
 
 
@@ -84,6 +99,7 @@ def run_calcite_kinetics(oracle, precision=0):
                            max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
     b = one_cell(net, fx, oracle)
     oracle.equilibrate_constraint(ns, copt, b, fx["constraint"]["types"], fx["constraint"]["conc"])
+    start_from_initial_condition(oracle, net, b)
     # GI steps: the totals at the start of each step are the previous state's totals
     sopt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_RELATIVE,
                            max_residual_tolerance=1e-15, max_relative_change_tolerance=0.0,
@@ -117,4 +133,104 @@ def run_ion_exchange_valocchi(oracle):
     for i, nm in enumerate(names):
         out[f"Total {nm}"] = b.total_out[i]
         out[f"Total Sorbed {nm}"] = b.total_sorb_eq[i]
+    return out, fx["gold"]
+
+
+def run_surface_complexation_1(oracle):
+    """surface-complexation-1 at time 0: constraint speciation (pH, charge
+    balance, totals) and the equilibrium surface complexes of one site
+    (RTotalSorbEqSurfCplx1, closed form: every complex binds one free site)."""
+    fx = load("kat_surface_complexation_1.json")
+    net = build_network(fx, oracle)
+    ns = net.as_struct()
+    copt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    b = one_cell(net, fx, oracle)
+    oracle.equilibrate_constraint(ns, copt, b, fx["constraint"]["types"], fx["constraint"]["conc"])
+    names = [p["name"] for p in fx["primaries"]]
+    gp, _ = oracle.activity_lag(ns, float(b.ionic_strength[0]), net.N, net.Nc)
+    act = b.pri_molal[:net.N] * gp
+    out = {"pH": -math.log10(act[0])}
+    for i, nm in enumerate(names):
+        out[f"Total {nm}"] = b.total_out[i]
+        out[f"Total Sorbed {nm}"] = b.total_sorb_eq[i]
+    sf = fx["surface"]
+    free = float(b.srfcplxrxn_free_site_conc[0])
+    out[f"Free {sf['site']}"] = free
+    for c in sf["complexes"]:
+        lnQK = -c["logK"][fx["temperatures"].index(25.0)] * LOG_TO_LN
+        for s_, v in c["stoich"]:
+            if s_ in names:
+                lnQK += v * math.log(act[names.index(s_)])
+        out[c["name"]] = free * math.exp(lnQK)
+    return out, fx["gold"]
+
+
+def _rtotal(net, m, gp, gs):
+    """RTotal (reaction.F90:4057-4158) for one cell in numpy: complex
+    molalities, component totals (mol/kg) and the ionic strength."""
+    lna = np.log(m) + np.log(gp)
+    C = np.zeros(net.Nc)
+    psi = m.copy()
+    for i, c in enumerate(net.complexes):
+        lnQK = -c.logK * LOG_TO_LN
+        for s_, v in zip(c.species, c.stoich):
+            lnQK += v * lna[net.idx(s_)]
+        C[i] = math.exp(lnQK) / gs[i]
+        for s_, v in zip(c.species, c.stoich):
+            psi[net.idx(s_)] += v * C[i]
+    zp = np.array(net.pri_Z)
+    zs = np.array([c.extra["Z"] for c in net.complexes])
+    I = 0.5 * (np.sum(zp * zp * m) + np.sum(zs * zs * C))
+    return C, psi, I
+
+
+def initial_condition_state(oracle, net, m, den_kg, act_coef_on):
+    """The state the reference reports at time 0 for a cell initialised from
+    a constraint when the constraint is equilibrated once and copied
+    (isothermal runs, condition_control.F90:600-700): the cell's own
+    activity coefficients start at 1, its auxiliary variables are computed
+    once without and, with activity coefficients on, twice with an activity
+    update (condition_control.F90:933-944).  Returns (gamma_pri, totals in
+    mol/L, ionic strength of the final complexes)."""
+    ns = net.as_struct()
+    gp, gs = np.ones(net.N), np.ones(net.Nc)
+    C, psi, I = _rtotal(net, m, gp, gs)
+    if act_coef_on:
+        for _ in range(2):
+            gp, gs = oracle.activity_lag(ns, I, net.N, net.Nc)
+            C, psi, I = _rtotal(net, m, gp, gs)
+    return gp, psi * den_kg * 1e-3, I
+
+
+def start_from_initial_condition(oracle, net, b):
+    """Replaces the constraint's final totals and ionic strength in the
+    host CellBatch `b` (cell 0) by the initialised cell's
+    (`initial_condition_state` with activity coefficients on): the state
+    the first time step starts from."""
+    m = b.pri_molal.reshape(net.N, -1)[:, 0].copy()
+    _, tot, I = initial_condition_state(oracle, net, m, float(b.den_kg[0]), True)
+    n = b.ncells
+    b.total_out.reshape(net.N, n)[:] = tot[:, None]
+    b.ionic_strength[:] = I
+
+
+def run_carbonate_speciation(oracle, deck):
+    """One of the carbonate speciation decks at time 0: constraint
+    speciation with TOTAL rows, unit or Debye-Hueckel activity."""
+    fx = load("kat_carbonate_speciation.json")[deck]
+    net = build_network(fx, oracle)
+    ns = net.as_struct()
+    freq = abi.ACT_COEF_FREQUENCY_OFF if fx["act_coef"] == "OFF" else abi.ACT_COEF_FREQUENCY_TIMESTEP
+    copt = default_options(use_isothermal=1, act_coef_update_frequency=freq, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    b = one_cell(net, fx, oracle)
+    oracle.equilibrate_constraint(ns, copt, b, fx["constraint"]["types"], fx["constraint"]["conc"])
+    names = [p["name"] for p in fx["primaries"]]
+    m = b.pri_molal[:net.N].copy()
+    gp, tot, _ = initial_condition_state(oracle, net, m, float(b.den_kg[0]), fx["act_coef"] != "OFF")
+    out = {"pH": -math.log10(m[names.index("H+")] * gp[names.index("H+")])}
+    for i, nm in enumerate(names):
+        out[f"Total {nm}"] = tot[i]
+        out[f"Gamma {nm}"] = gp[i]
     return out, fx["gold"]

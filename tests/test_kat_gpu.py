@@ -47,12 +47,14 @@ def test_ion_exchange_valocchi_gold_gpu(oracle):
 
 
 def test_calcite_kinetics_gold_gpu(oracle):
-    """Constraint speciation and 500 reaction steps of 0.5 s on the GPU."""
+    """Constraint speciation on the GPU, the reference's initialisation of
+    the cell, then 500 reaction steps of 0.5 s on the GPU."""
     fx = kat.load("kat_calcite_kinetics.json")
     net = kat.build_network(fx, oracle)
     copt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
                            max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
     g = _constraint_on_gpu(net, copt, kat.one_cell(net, fx, oracle), fx, ncopies=32)
+    kat.start_from_initial_condition(oracle, net, g)
     d = g.to_device()
     sopt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_RELATIVE, max_residual_tolerance=1e-15,
                            max_relative_change_tolerance=0.0, max_iterations=100, update_kinetic_state=1)
@@ -71,4 +73,27 @@ def test_calcite_kinetics_gold_gpu(oracle):
     for key, v in out.items():
         assert np.abs(v - fx["gold"][key]).max() <= 1e-12, (key, v[0], fx["gold"][key])
     ph = -math.log10(h.pri_molal[0] * gp[0])
-    assert abs(ph - fx["gold"]["pH"]) <= 5e-8
+    assert abs(ph - fx["gold"]["pH"]) <= 1e-12
+
+
+def test_surface_complexation_1_gold_gpu(oracle):
+    """surface-complexation-1 at time 0 (pH and charge-balance rows, one
+    equilibrium surface-complexation site) solved on the GPU: aqueous totals
+    within 1e-12 absolute, free sites and sorbed totals (up to 7.6e4
+    mol/m^3, 14 printed digits) within 1e-12 relative."""
+    fx = kat.load("kat_surface_complexation_1.json")
+    net = kat.build_network(fx, oracle)
+    copt = default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                           max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    g = _constraint_on_gpu(net, copt, kat.one_cell(net, fx, oracle), fx)
+    names = [p["name"] for p in fx["primaries"]]
+    n = g.ncells
+    gold = fx["gold"]
+    for i, nm in enumerate(names):
+        v = g.total_out.reshape(net.N, n)[i]
+        assert np.abs(v - gold[f"Total {nm}"]).max() <= 1e-12, (nm, v[0], gold[f"Total {nm}"])
+        v = g.total_sorb_eq.reshape(net.N, n)[i]
+        ref = gold[f"Total Sorbed {nm}"]
+        assert np.abs(v - ref).max() <= 1e-12 * max(abs(ref), 1.0), (nm, v[0], ref)
+    free = g.srfcplxrxn_free_site_conc.reshape(-1, n)[0]
+    assert np.abs(free - gold["Free >FeOH_w"]).max() <= 1e-12 * gold["Free >FeOH_w"]

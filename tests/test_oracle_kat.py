@@ -26,14 +26,13 @@ def test_ion_exchange_valocchi_gold(oracle):
 
 @pytest.mark.parametrize("precision", [0, 1])
 def test_calcite_kinetics_gold(oracle, precision):
-    """calcite-kinetics: 500 steps of 0.5 s of RTotal + LAG activity (TIMESTEP) +
-    RKineticMineral + RUpdateKineticState.  Totals, calcite volume fraction and
-    rate meet the harness's 1e-12 absolute; pH (which depends on which state's
-    ionic strength the output's activity coefficient used) is held to 5e-8."""
+    """calcite-kinetics: the initialised constraint state, then 500 steps of
+    0.5 s of RTotal + LAG activity (TIMESTEP) + RKineticMineral +
+    RUpdateKineticState.  Totals, calcite volume fraction, rate and pH meet
+    the harness's 1e-12 absolute."""
     out, gold = kat.run_calcite_kinetics(oracle, precision)
-    for key in ("Total H+", "Total HCO3-", "Total Ca++", "Calcite VF", "Calcite Rate"):
+    for key in ("Total H+", "Total HCO3-", "Total Ca++", "Calcite VF", "Calcite Rate", "pH"):
         assert abs(out[key] - gold[key]) <= 1e-12, (key, out[key], gold[key])
-    assert abs(out["pH"] - gold["pH"]) <= 5e-8
 
 
 def test_rsolve_matches_dense_solve(oracle):
@@ -133,3 +132,30 @@ def test_constraint_rows_are_satisfied(oracle):
     lnQK = -mn.logK * 2.30258509299 + sum(nu * np.log(m[net.idx(s)] * gp[net.idx(s)])
                                          for s, nu in zip(mn.species, mn.stoich))
     assert np.abs(lnQK).max() < 1e-6
+
+
+def test_surface_complexation_1_gold(oracle):
+    """surface-complexation-1 (time 0): constraint speciation with pH and
+    charge-balance rows + one equilibrium surface-complexation site
+    (7.6355e4 mol/m^3, three complexes).  The harness's 1e-12 absolute is
+    met on the aqueous totals; the sorbed quantities (up to 7.6e4 mol/m^3,
+    printed to 14 digits) are held to 1e-12 relative."""
+    out, gold = kat.run_surface_complexation_1(oracle)
+    for key in ("Total H+", "Total Na+", "Total NO3-", "Total Zn++"):
+        assert abs(out[key] - gold[key]) <= 1e-12, (key, out[key], gold[key])
+    for key in ("Free >FeOH_w", ">FeOH2+_w", ">FeO-_w", ">FeOHZn+_w", "Total Sorbed H+", "Total Sorbed Na+",
+                "Total Sorbed NO3-", "Total Sorbed Zn++"):
+        assert abs(out[key] - gold[key]) <= 1e-12 * max(abs(gold[key]), 1.0), (key, out[key], gold[key])
+    assert abs(out["pH"] - gold["pH"]) <= 1e-8
+
+
+@pytest.mark.parametrize("deck", ["carbonate-unit-activity", "carbonate-debye-huckel-activity",
+                                  "ca-carbonate-unit-activity", "ca-carbonate-debye-huckel-activity"])
+def test_carbonate_speciation_gold(oracle, deck):
+    """The carbonate speciation decks at time 0 (constraint speciation with
+    TOTAL rows, unit or Debye-Hueckel activity, then the reference's
+    initialisation of the cell): pH, totals and activity coefficients
+    within the harness's 1e-12 absolute."""
+    out, gold = kat.run_carbonate_speciation(oracle, deck)
+    for key, v in out.items():
+        assert abs(v - gold[key]) <= 1e-12, (key, v, gold[key])
