@@ -8,6 +8,7 @@ Run in a checkout that has the PFLOTRAN source tree (argument: its root):
 It reads, as text, the database rows and the regression gold values of
 
   regression_tests/ascem/batch/calcite-kinetics.{in,regression.gold} + calcite.dat
+  regression_tests/ascem/batch/calcite-kinetics-volume-fractions.{in,regression.gold}
   regression_tests/ascem/batch/ion-exchange-valocchi.{in,regression.gold} + hanford.dat
   regression_tests/ascem/batch/surface-complexation-1.{in,regression.gold}
       + surface-complexation.dat
@@ -114,6 +115,17 @@ def main(root):
     )
     with open(os.path.join(HERE, "kat_calcite_kinetics.json"), "w") as f:
         json.dump(fx, f, indent=1)
+    # calcite-kinetics-volume-fractions: the same deck but for the time
+    # card (FINAL_TIME 60 mo = 60 x 365/12 d, units.F90:445-446; initial and
+    # maximum step 30 d) and the constraint (H+ 1e-2, HCO3- 1e-2, Ca++ 1e-19 T)
+    vf = dict(fx)
+    vf.update(source="regression_tests/ascem/batch/calcite-kinetics-volume-fractions.in + calcite.dat "
+                     "+ .regression.gold",
+              final_time=60 * 365.0 / 12.0 * 86400.0, dt=30.0 * 86400.0, nsteps=None,
+              constraint=dict(types=[1, 1, 1], conc=[1e-2, 1e-2, 1e-19]),
+              gold=read_gold(os.path.join(batch, "calcite-kinetics-volume-fractions.regression.gold")))
+    with open(os.path.join(HERE, "kat_calcite_kinetics_volume_fractions.json"), "w") as f:
+        json.dump(vf, f, indent=1)
     # --- ion-exchange-valocchi ----------------------------------------------
     pri = ["Na+", "Ca++", "Mg++", "Cl-"]
     temps, rows = read_dat(os.path.join(batch, "hanford.dat"), set(pri + ["Halite"]))

@@ -90,8 +90,20 @@ def one_cell(net, fx, oracle):
     return b
 
 
-def run_calcite_kinetics(oracle, precision=0):
-    fx = load("kat_calcite_kinetics.json")
+def step_sizes(fx):
+    """The deck's time steps: `nsteps` of `dt`, or steps of `dt` up to
+    `final_time` with the last one shortened to land on it."""
+    if fx.get("nsteps"):
+        return [fx["dt"]] * fx["nsteps"]
+    out, t = [], 0.0
+    while fx["final_time"] - t > 1e-6 * fx["dt"]:
+        out.append(min(fx["dt"], fx["final_time"] - t))
+        t += out[-1]
+    return out
+
+
+def run_calcite_kinetics(oracle, precision=0, fixture="kat_calcite_kinetics.json"):
+    fx = load(fixture)
     net = build_network(fx, oracle)
     ns = net.as_struct()
     # constraint speciation (relative-change and residual tolerances of the deck: defaults)
@@ -105,10 +117,10 @@ def run_calcite_kinetics(oracle, precision=0):
                            max_residual_tolerance=1e-15, max_relative_change_tolerance=0.0,
                            max_iterations=100, update_kinetic_state=1)
     I_prev = float(b.ionic_strength[0])
-    for step in range(fx["nsteps"]):
+    for dt in step_sizes(fx):
         b.total[:] = b.total_out
         I_prev = float(b.ionic_strength[0])
-        bad = oracle.react(ns, sopt, fx["dt"], b, precision, 1)
+        bad = oracle.react(ns, sopt, dt, b, precision, 1)
         assert bad == 0, b.status
     gp, _ = oracle.activity_lag(ns, I_prev, net.N, net.Nc)
     out = {
