@@ -18,11 +18,25 @@ log K(T) = c1 ln T_K + c2 + c3 T_K + c4 / T_K + c5 / T_K^2 over the
 temperatures with data.
 
 `network_from_database` builds a ReactionNetwork for a chosen set of primary
-species in the database's own basis: every secondary species, mineral and
-surface complex must be written in terms of the chosen primaries (and
-H2O).  PFLOTRAN's basis swap (reaction_database.F90:772-, which rewrites
-reactions for a different basis) is not done: a species whose reaction
-uses a component that is not among the primaries (e.g. redox couples
+species.  When that set is not the database's own basis (a primary that the
+database lists as a secondary species, e.g. CO2(aq) instead of HCO3-), the
+reactions are rewritten for the new basis as BasisInit does
+(reaction_database.F90:772-1560): every reaction of a chosen primary or
+secondary species that the database defines is a row of
+  pri . P + sec . S = log K
+over the basis P (H2O and the primaries) and the secondary species S; with
+the secondary block inverted, each secondary species becomes
+S = -sec^-1 pri . P with log K = -sec^-1 . log K, and every secondary species
+left in a mineral or surface-complex reaction is replaced by its rewritten
+reaction, scaled by its coefficient there, log K likewise
+(BasisSubSpeciesInMineralRxn / BasisSubSpeciesInGasOrSecRxn,
+reaction_database_aux.F90:355-545).  Differences, deliberate: the secondary
+block is solved with numpy instead of ludcmp/lubksb (log K agrees to
+rounding); a rewritten log K at a temperature where any reaction it combines
+has no data is marked as no data (500) instead of being combined; and
+rewritten coefficients within 1e-12 of an integer are snapped to it, so
+that a swap does not leave 1e-16 coefficients in the kinetic tables.  Gas
+species are not supported: a reaction that needs one (e.g. redox couples
 written with O2(g)) is rejected with a message naming it.
 """
 from __future__ import annotations
@@ -186,13 +200,124 @@ def logK_at_25(db, rx):
     return k
 
 
+def _has_data(k):
+    return abs(k - NO_DATA) > 1e-10
+
+
+def _combine(terms, ntemp):
+    """sum of scale * logK vectors over (scale, logK) terms, per temperature;
+    no data where any term with a nonzero scale has none."""
+    out = []
+    for t in range(ntemp):
+        if any(abs(c) > 0 and not _has_data(k[t]) for c, k in terms):
+            out.append(NO_DATA)
+        else:
+            out.append(sum(c * k[t] for c, k in terms))
+    return out
+
+
+def _snap(v):
+    r = round(v)
+    return float(r) if abs(v - r) <= 1e-12 else float(v)
+
+
+def swap_basis(db, primaries, secondary):
+    """Reactions of the `secondary` species written in the basis H2O +
+    `primaries` (the BasisInit rewrite): {name: (stoich {species: nu},
+    logK per database temperature, a0, Z)}."""
+    basis = ["H2O"] + list(primaries)
+    bidx = {n: i for i, n in enumerate(basis)}
+    sidx = {n: i for i, n in enumerate(secondary)}
+    for n in primaries:
+        if n in sidx:
+            raise ValueError(f"{n} is listed as both a primary and a secondary species")
+    rows = []   # (self name, database reaction)
+    for n in primaries:
+        if n not in db.primaries:
+            if n not in db.secondary:
+                raise ValueError(f"primary species {n} is in neither the database's primary nor secondary species")
+            rows.append((n, db.secondary[n]))
+    for n in secondary:
+        if n in db.secondary:
+            rows.append((n, db.secondary[n]))
+        elif n not in db.primaries:
+            raise ValueError(f"secondary species {n} is not in the database")
+    ns = len(secondary)
+    if len(rows) != ns:
+        raise ValueError(f"{len(rows)} reactions from the database for {ns} secondary species: the primaries "
+                         f"and secondaries do not span the same components as the database's basis")
+    pri = np.zeros((ns, len(basis)))
+    sec = np.zeros((ns, ns))
+    nt = len(db.temperatures)
+    logK = np.zeros((ns, nt))
+    for r, (n, rx) in enumerate(rows):
+        if n in bidx:
+            pri[r, bidx[n]] = -1.0
+        else:
+            sec[r, sidx[n]] = -1.0
+        for sp, nu in rx.stoich:
+            if sp in bidx:
+                pri[r, bidx[sp]] += nu
+            elif sp in sidx:
+                sec[r, sidx[sp]] += nu
+            else:
+                raise ValueError(f"species {sp} in the reaction of {n} is not among the primary or secondary "
+                                 f"species (gases and basis swaps through them are not supported)")
+        logK[r] = rx.logK
+    try:
+        inv = np.linalg.inv(sec)
+    except np.linalg.LinAlgError:
+        raise ValueError("the secondary species' reactions are not independent in this basis") from None
+    stoich = -inv @ pri
+    own = {n: rx for n, rx in rows}
+    out = {}
+    for k, n in enumerate(secondary):
+        st = {basis[j]: _snap(v) for j, v in enumerate(stoich[k]) if abs(v) > 1e-10}
+        if n in own:  # keep the database's species order, then the basis order
+            first = [sp for sp, _ in own[n].stoich if sp in st]
+            st = {sp: st[sp] for sp in first + [sp for sp in st if sp not in first]}
+        lk = _combine([(-inv[k, r], logK[r]) for r in range(ns)], nt)
+        if n in db.primaries:
+            a0, Z = db.primaries[n]
+        else:
+            a0, Z = db.secondary[n].a0, db.secondary[n].Z
+        out[n] = (st, lk, a0, Z)
+    return out
+
+
+def rewrite_in_basis(rx_stoich, rx_logK, swapped, basis, what):
+    """A mineral or surface-complex reaction with every secondary species in
+    it replaced by its rewritten reaction (scaled by its coefficient), log K
+    likewise; species whose coefficients cancel (|nu| <= 1e-10) are dropped.
+    Raises when a species is left that is not in `basis` (plus surface
+    sites, names starting with '>')."""
+    st = dict()
+    for sp, nu in rx_stoich:
+        st[sp] = st.get(sp, 0.0) + nu
+    terms = [(1.0, list(rx_logK))]
+    for sp in list(st):
+        if sp in swapped and sp not in basis:
+            scale = st.pop(sp)
+            s2, lk2, _, _ = swapped[sp]
+            for q, v in s2.items():
+                st[q] = st.get(q, 0.0) + scale * v
+            terms.append((scale, lk2))
+    st = {q: _snap(v) for q, v in st.items() if abs(v) > 1e-10}
+    bad = [q for q in st if q not in basis and not q.startswith(">")]
+    if bad:
+        raise ValueError(f"{what}: reaction uses {bad}, not among the primaries or the secondary species")
+    return [(q, v) for q, v in st.items()], _combine(terms, len(rx_logK))
+
+
 def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, ion_exchange=None,
                           surface_complexation=None, debye=None):
-    """ReactionNetwork for `primaries` (names in the database's basis).
+    """ReactionNetwork for `primaries` (the database's basis or another one,
+    rewritten as the module notes describe).
 
-    secondary: names of the aqueous complexes, or None for every secondary
-      species whose reaction uses only the primaries and H2O (PFLOTRAN lists
-      them in the input deck; this is the usual "all that apply");
+    secondary: names of the aqueous complexes, or, in the database's own
+      basis, None for every secondary species whose reaction uses only the
+      primaries and H2O (PFLOTRAN lists them in the input deck; this is the
+      usual "all that apply");
     kinetic_minerals: {name: dict(rate_constant=mol/m^2/s, ...)} with the
       other add_kinetic_mineral keywords;
     ion_exchange: [(cations with selectivities [(name, k)], CEC)];
@@ -200,36 +325,48 @@ def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, 
     Log K is the 25 C value; the temperature fit is attached when the
     database has five or more temperatures with data."""
     from .network import ReactionNetwork
-    prim = [(p, db.primaries[p][1], db.primaries[p][0]) for p in primaries]
+
+    def primary_params(p):
+        if p in db.primaries:
+            return db.primaries[p][1], db.primaries[p][0]
+        rx = db.secondary[p] if p in db.secondary else None
+        if rx is None:
+            raise ValueError(f"primary species {p} is not in the database")
+        return rx.Z, rx.a0
+
+    prim = [(p, *primary_params(p)) for p in primaries]
     net = ReactionNetwork(prim, **({} if debye is None else {"debye": debye}))
     allowed = set(primaries) | {"H2O"}
-
-    def check(rx, what):
-        bad = [s for s, _ in rx.stoich if s not in allowed]
-        if bad:
-            raise ValueError(f"{what} {rx.name}: reaction uses {bad}, not among the primaries "
-                             f"(a basis swap is not supported)")
-
+    swap = any(p not in db.primaries for p in primaries)
     if secondary is None:
+        if swap:
+            raise ValueError("a basis other than the database's needs the secondary species listed")
         names = [n for n, rx in db.secondary.parsable()
                  if n not in allowed and all(s in allowed for s, _ in rx.stoich) and
-                 abs(rx.logK[db.temperatures.index(25.0)] - NO_DATA) > 1e-10]
+                 _has_data(rx.logK[db.temperatures.index(25.0)])]
     else:
         names = list(secondary)
+    swapped = swap_basis(db, primaries, names)
+    t25 = db.temperatures.index(25.0)
+
+    def fit(lk):
+        return fit_logK(db.temperatures, lk)
+
+    def at25(lk, what):
+        if not _has_data(lk[t25]):
+            raise ValueError(f"{what}: no log K at 25 C")
+        return lk[t25]
+
     for n in names:
-        rx = db.secondary[n]
-        check(rx, "secondary species")
-        st = {s: v for s, v in rx.stoich if s != "H2O"}
-        h2o = sum(v for s, v in rx.stoich if s == "H2O")
-        net.add_complex(n, st, logK=logK_at_25(db, rx), Z=rx.Z, a0=rx.a0,
-                        logKcoef=fit_logK(db.temperatures, rx.logK), h2o=h2o)
+        st, lk, a0, Z = swapped[n]
+        net.add_complex(n, {s: v for s, v in st.items() if s != "H2O"}, logK=at25(lk, n), Z=Z, a0=a0,
+                        logKcoef=fit(lk), h2o=st.get("H2O", 0.0))
     for n, kw in (kinetic_minerals or {}).items():
         rx = db.minerals[n]
-        check(rx, "mineral")
-        st = {s: v for s, v in rx.stoich if s != "H2O"}
+        st, lk = rewrite_in_basis(rx.stoich, rx.logK, swapped, allowed, f"mineral {n}")
         kw = dict(kw)
         kw.setdefault("molar_vol", rx.molar_vol_cm3 * 1e-6)
-        net.add_kinetic_mineral(n, st, logK=logK_at_25(db, rx), logKcoef=fit_logK(db.temperatures, rx.logK), **kw)
+        net.add_kinetic_mineral(n, {s: v for s, v in st if s != "H2O"}, logK=at25(lk, n), logKcoef=fit(lk), **kw)
     for cations, cec in (ion_exchange or []):
         net.add_ion_exchange(cations, cec)
     for site_density, complexes, kw in (surface_complexation or []):
@@ -237,14 +374,12 @@ def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, 
         for n in complexes:
             rx = db.surface_complexes[n]
             sites = [s for s, _ in rx.stoich if s.startswith(">")]
-            rest = {s: v for s, v in rx.stoich if not s.startswith(">") and s != "H2O"}
-            bad = [s for s in rest if s not in allowed]
-            if bad:
-                raise ValueError(f"surface complex {n}: reaction uses {bad}, not among the primaries")
             if len(set(sites)) != 1:
                 raise ValueError(f"surface complex {n}: expected one surface site, found {sites}")
-            fs = sum(v for s, v in rx.stoich if s.startswith(">"))
-            cplx.append((rest, fs, logK_at_25(db, rx)))
+            st, lk = rewrite_in_basis(rx.stoich, rx.logK, swapped, allowed, f"surface complex {n}")
+            rest = {s: v for s, v in st if not s.startswith(">") and s != "H2O"}
+            fs = sum(v for s, v in st if s.startswith(">"))
+            cplx.append((rest, fs, at25(lk, n)))
         net.add_surface_complexation(site_density, cplx, **kw)
     net.build()
     return net

@@ -81,5 +81,102 @@ def test_reads_reference_database():
                                          kinetic_minerals={"Calcite": dict(rate_constant=1e-9)})
     names = [c.extra["name"] for c in net.complexes]
     assert "OH-" in names and "CO2(aq)" in names and "CaCO3(aq)" in names
-    with pytest.raises(ValueError, match="basis swap"):
+    # a swapped basis on the full database: CO2(aq) primary, HCO3- secondary
+    sec = ["OH-", "CO3--", "HCO3-", "CaOH+", "CaHCO3+", "CaCO3(aq)"]
+    net2 = database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"], secondary=sec,
+                                          kinetic_minerals={"Calcite": dict(rate_constant=1e-9)})
+    calcite = net2.minerals[0]
+    assert dict(zip(calcite.species, calcite.stoich)) == {"H+": -2.0, "Ca++": 1.0, "CO2(aq)": 1.0}
+    # redox couples written with O2(g): gases are not supported
+    with pytest.raises(ValueError, match="gases"):
         database.network_from_database(db, ["H+", "SO4--"], secondary=["HS-"])
+
+
+LN10 = np.log(10.0)
+
+
+def _ln_activities(net, lna_pri):
+    """ln activity of every species at unit activity coefficients: the
+    primaries' given values and each complex from its mass action."""
+    out = dict(zip(net.pri_names, lna_pri))
+    for c in net.complexes:
+        out[c.extra["name"]] = -c.logK * LN10 + sum(v * out[s] for s, v in zip(c.species, c.stoich))
+    return out
+
+
+def _ln_QK(net, ln_a):
+    return {m.extra["name"]: -m.logK * LN10 + sum(v * ln_a[s] for s, v in zip(m.species, m.stoich))
+            for m in net.minerals}
+
+
+def _calcite_networks(tmp_path):
+    path = tmp_path / "calcite.dat"
+    fx = _write_small_db(path)
+    db = database.read_database(path)
+    sec = [c["name"] for c in fx["complexes"]]
+    kin = {"Calcite": dict(rate_constant=1e-9)}
+    a = database.network_from_database(db, ["H+", "HCO3-", "Ca++"], secondary=sec, kinetic_minerals=kin)
+    # CO2(aq) as a primary instead of HCO3- (a database secondary species)
+    sec_b = [s for s in sec if s != "CO2(aq)"] + ["HCO3-"]
+    b = database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"], secondary=sec_b, kinetic_minerals=kin)
+    return db, a, b
+
+
+def test_basis_swap_preserves_mass_action(tmp_path):
+    """The same solution described in two bases: every species' activity and
+    the calcite saturation agree whichever species are primary."""
+    db, a, b = _calcite_networks(tmp_path)
+    co2 = next(c for c in b.complexes if c.extra["name"] == "HCO3-")
+    # HCO3- = CO2(aq) + H2O - H+ with log K = -log K(CO2(aq)) in the database's direction
+    assert dict(zip(co2.species, co2.stoich)) == {"CO2(aq)": 1.0, "H+": -1.0} and co2.h2o == 1.0
+    assert abs(co2.logK + db.secondary["CO2(aq)"].logK[1]) < 1e-12
+    rng = np.random.default_rng(5)
+    for _ in range(20):
+        la = _ln_activities(a, rng.uniform(-12.0, -1.0, 3))
+        lb = _ln_activities(b, np.array([la["H+"], la["CO2(aq)"], la["Ca++"]]))
+        for name, v in la.items():
+            assert abs(lb[name] - v) < 1e-11, name
+        qa, qb = _ln_QK(a, la), _ln_QK(b, lb)
+        assert abs(qa["Calcite"] - qb["Calcite"]) < 1e-11
+
+
+def test_basis_swap_through_the_oracle(oracle, tmp_path):
+    """Free-ion constraint speciation in both bases from the same free-ion
+    state, through the oracle's tables: the same species concentrations.
+    (Unit activity coefficients: the constraint's lagged activity update
+    stops after two updates, so with Debye-Hueckel the two bases would
+    stop at different points of the same fixed-point iteration.)"""
+    from pflotran_gb300 import abi
+    from pflotran_gb300.network import default_options
+    db, a, b = _calcite_networks(tmp_path)
+    fx = kat.load("kat_calcite_kinetics.json")
+    opt = default_options(use_isothermal=1, act_coef_update_frequency=abi.ACT_COEF_FREQUENCY_OFF,
+                          residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                          max_relative_change_tolerance=1e-12, max_residual_tolerance=1e-14)
+    ca = kat.one_cell(a, fx, oracle)
+    molar = [1e-7, 2e-3, 1e-3]  # H+, HCO3-, Ca++ free (mol/L)
+    oracle.equilibrate_constraint(a.as_struct(), opt, ca, [2, 2, 2], molar)
+    conc_a = dict(zip(a.pri_names, ca.pri_molal[:3]))
+    conc_a.update({c.extra["name"]: ca.sec_molal[i] for i, c in enumerate(a.complexes)})
+    den = float(ca.den_kg[0]) * 1e-3
+    cb = kat.one_cell(b, fx, oracle)
+    oracle.equilibrate_constraint(b.as_struct(), opt, cb, [2, 2, 2],
+                                  [conc_a["H+"] * den, conc_a["CO2(aq)"] * den, conc_a["Ca++"] * den])
+    conc_b = dict(zip(b.pri_names, cb.pri_molal[:3]))
+    conc_b.update({c.extra["name"]: cb.sec_molal[i] for i, c in enumerate(b.complexes)})
+    for name, v in conc_a.items():
+        assert abs(conc_b[name] - v) <= 1e-12 * v, (name, conc_b[name], v)
+
+
+def test_basis_swap_rejects_inconsistent_bases(tmp_path):
+    path = tmp_path / "calcite.dat"
+    fx = _write_small_db(path)
+    db = database.read_database(path)
+    sec = [c["name"] for c in fx["complexes"]]
+    with pytest.raises(ValueError, match="secondary species listed"):
+        database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"])
+    with pytest.raises(ValueError, match="span the same components"):
+        # CO2(aq) primary but HCO3- missing from the secondaries: one reaction too many
+        database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"], secondary=[s for s in sec if s != "CO2(aq)"])
+    with pytest.raises(ValueError, match="both a primary and a secondary"):
+        database.network_from_database(db, ["H+", "HCO3-", "Ca++"], secondary=sec + ["HCO3-"])
