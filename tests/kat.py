@@ -246,3 +246,88 @@ def run_carbonate_speciation(oracle, deck):
         out[f"Total {nm}"] = tot[i]
         out[f"Gamma {nm}"] = gp[i]
     return out, fx["gold"]
+
+
+def write_calcite_db(path):
+    """A database in PFLOTRAN's format with the calcite system's rows as the
+    known-answer fixture records them."""
+    fx = load("kat_calcite_kinetics.json")
+    temps = fx["temperatures"]
+    q = lambda s: f"'{s}'"
+    lines = [f"'temperature points' {len(temps)} " + " ".join(str(t) for t in temps)]
+    for p in fx["primaries"]:
+        lines.append(f"{q(p['name'])} {p['a0']} {p['Z']} 1.0")
+    lines.append("'null' 0 0 0")
+    for c in fx["complexes"]:
+        st = " ".join(f"{v} {q(s)}" for s, v in c["stoich"])
+        lines.append(f"{q(c['name'])} {len(c['stoich'])} {st} " + " ".join(str(k) for k in c["logK"]) +
+                     f" {c['a0']} {c['Z']} 1.0")
+    lines.append("'null' 1 0. '0' " + " ".join("0." for _ in temps))
+    lines.append("'null' 0. 1 0. '0' " + " ".join("0." for _ in temps))
+    for m in fx["minerals"]:
+        st = " ".join(f"{v} {q(s)}" for s, v in m["stoich"])
+        lines.append(f"{q(m['name'])} {m['molar_vol_cm3']} {len(m['stoich'])} {st} " +
+                     " ".join(str(k) for k in m["logK"]) + " 100.0")
+    lines.append("'null' 0. 1 0. '0' " + " ".join("0." for _ in temps))
+    lines.append("'null' 1 0. '0' " + " ".join("0." for _ in temps))
+    with open(path, "w") as f:
+        f.write("\n".join(lines) + "\n")
+    return fx
+
+
+def calcite_networks_two_bases(db_path):
+    """The calcite system from the database written by write_calcite_db in
+    its own basis (H+, HCO3-, Ca++) and with CO2(aq) primary instead of
+    HCO3- (basis swap), kinetic calcite in both."""
+    from pflotran_gb300 import database
+    fx = write_calcite_db(db_path)
+    db = database.read_database(db_path)
+    sec = [c["name"] for c in fx["complexes"]]
+    kin = {"Calcite": dict(rate_constant=1e-9)}
+    a = database.network_from_database(db, ["H+", "HCO3-", "Ca++"], secondary=sec, kinetic_minerals=kin,
+                                       debye=debye_25C())
+    sec_b = [s for s in sec if s != "CO2(aq)"] + ["HCO3-"]
+    b = database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"], secondary=sec_b, kinetic_minerals=kin,
+                                       debye=debye_25C())
+    return db, a, b
+
+
+def species_molalities(oracle, net, cells):
+    """Molality of every species of each cell (primaries: the state's free
+    ions; complexes: mass action with LAG activity coefficients at the
+    cell's ionic strength): {name: array over cells}."""
+    n = cells.ncells
+    m = cells.pri_molal.reshape(net.N, n)
+    out = {nm: m[j].copy() for j, nm in enumerate(net.pri_names)}
+    for c in net.complexes:
+        out[c.extra["name"]] = np.zeros(n)
+    ns = net.as_struct()
+    for k in range(n):
+        gp, gs = oracle.activity_lag(ns, float(cells.ionic_strength[k]), net.N, net.Nc)
+        lna = np.log(m[:, k]) + np.log(gp)
+        for i, c in enumerate(net.complexes):
+            ln = -c.logK * LOG_TO_LN + sum(v * lna[net.idx(s)] for s, v in zip(c.species, c.stoich))
+            out[c.extra["name"]][k] = math.exp(ln) / gs[i]
+    return out
+
+
+def cells_in_basis(oracle, net_a, net_b, cells_a):
+    """The cells of `net_a` described in the basis of `net_b` (same species,
+    other primaries).  Every species is the same combination of either
+    basis's components, so the component totals map linearly: net_b's total
+    of component k = sum_j (net_b composition of net_a's primary j)_k x
+    net_a's total j.  The free-ion guess is the species' molalities."""
+    n = cells_a.ncells
+    conc = species_molalities(oracle, net_a, cells_a)
+    comp = {nm: {nm: 1.0} for nm in net_b.pri_names}
+    for c in net_b.complexes:
+        comp[c.extra["name"]] = dict(zip(c.species, c.stoich))
+    conv = np.zeros((net_b.N, net_a.N))
+    for j, nm in enumerate(net_a.pri_names):
+        for s, v in comp[nm].items():
+            conv[net_b.idx(s), j] += v
+    b = cells_a.copy()
+    b.total = np.ascontiguousarray((conv @ cells_a.total.reshape(net_a.N, n)).ravel())
+    b.pri_molal = np.ascontiguousarray(np.stack([conc[nm] for nm in net_b.pri_names]).ravel())
+    b.sec_molal = np.zeros(max(net_b.Nc, 1) * n)
+    return b

@@ -10,36 +10,9 @@ from pflotran_gb300 import database
 REF_DB = "/root/reference/database/hanford.dat"
 
 
-def _write_small_db(path):
-    """A database in PFLOTRAN's format with the calcite system's rows as the
-    known-answer fixture records them."""
-    fx = kat.load("kat_calcite_kinetics.json")
-    temps = fx["temperatures"]
-    q = lambda s: f"'{s}'"
-    lines = [f"'temperature points' {len(temps)} " + " ".join(str(t) for t in temps)]
-    for p in fx["primaries"]:
-        lines.append(f"{q(p['name'])} {p['a0']} {p['Z']} 1.0")
-    lines.append("'null' 0 0 0")
-    for c in fx["complexes"]:
-        st = " ".join(f"{v} {q(s)}" for s, v in c["stoich"])
-        lines.append(f"{q(c['name'])} {len(c['stoich'])} {st} " + " ".join(str(k) for k in c["logK"]) +
-                     f" {c['a0']} {c['Z']} 1.0")
-    lines.append("'null' 1 0. '0' " + " ".join("0." for _ in temps))
-    lines.append("'null' 0. 1 0. '0' " + " ".join("0." for _ in temps))
-    for m in fx["minerals"]:
-        st = " ".join(f"{v} {q(s)}" for s, v in m["stoich"])
-        lines.append(f"{q(m['name'])} {m['molar_vol_cm3']} {len(m['stoich'])} {st} " +
-                     " ".join(str(k) for k in m["logK"]) + " 100.0")
-    lines.append("'null' 0. 1 0. '0' " + " ".join("0." for _ in temps))
-    lines.append("'null' 1 0. '0' " + " ".join("0." for _ in temps))
-    with open(path, "w") as f:
-        f.write("\n".join(lines) + "\n")
-    return fx
-
-
 def test_network_from_database_matches_fixture_network(oracle, tmp_path):
     path = tmp_path / "calcite.dat"
-    fx = _write_small_db(path)
+    fx = kat.write_calcite_db(path)
     db = database.read_database(path)
     prim = [p["name"] for p in fx["primaries"]]
     net = database.network_from_database(
@@ -111,7 +84,7 @@ def _ln_QK(net, ln_a):
 
 def _calcite_networks(tmp_path):
     path = tmp_path / "calcite.dat"
-    fx = _write_small_db(path)
+    fx = kat.write_calcite_db(path)
     db = database.read_database(path)
     sec = [c["name"] for c in fx["complexes"]]
     kin = {"Calcite": dict(rate_constant=1e-9)}
@@ -170,7 +143,7 @@ def test_basis_swap_through_the_oracle(oracle, tmp_path):
 
 def test_basis_swap_rejects_inconsistent_bases(tmp_path):
     path = tmp_path / "calcite.dat"
-    fx = _write_small_db(path)
+    fx = kat.write_calcite_db(path)
     db = database.read_database(path)
     sec = [c["name"] for c in fx["complexes"]]
     with pytest.raises(ValueError, match="secondary species listed"):
@@ -180,3 +153,31 @@ def test_basis_swap_rejects_inconsistent_bases(tmp_path):
         database.network_from_database(db, ["H+", "CO2(aq)", "Ca++"], secondary=[s for s in sec if s != "CO2(aq)"])
     with pytest.raises(ValueError, match="both a primary and a secondary"):
         database.network_from_database(db, ["H+", "HCO3-", "Ca++"], secondary=sec + ["HCO3-"])
+
+
+def test_reaction_step_is_the_same_in_a_swapped_basis(oracle, tmp_path):
+    """The calcite workload stepped by the oracle in the database's basis
+    and, re-expressed, with CO2(aq) primary: after the step every species'
+    molality agrees to 1e-9 (measured 2e-11: each basis converges its own
+    component residuals to 1e-12), the volume fractions to 1e-12 and the
+    calcite rate to 5e-9 of k x area (measured 9e-10: near equilibrium the
+    affinity 1 - Q/K turns the species' 1e-11 into ~1e-9)."""
+    from pflotran_gb300 import workloads
+    db, a, b = kat.calcite_networks_two_bases(tmp_path / "calcite.dat")
+    _, opt, ca, dt = workloads.calcite_cells(256, seed=9, net=a)
+    ca.sec_molal = np.zeros(a.Nc * ca.ncells)
+    cb = kat.cells_in_basis(oracle, a, b, ca)
+    ra, rb = ca.copy(), cb.copy()
+    assert oracle.react(a.as_struct(), opt, dt, ra, 0, 4) == 0
+    assert oracle.react(b.as_struct(), opt, dt, rb, 0, 4) == 0
+    n = ra.ncells
+    sa = dict(zip(a.pri_names, ra.pri_molal.reshape(a.N, n)))
+    sa.update({c.extra["name"]: ra.sec_molal.reshape(-1, n)[i] for i, c in enumerate(a.complexes)})
+    sb = dict(zip(b.pri_names, rb.pri_molal.reshape(b.N, n)))
+    sb.update({c.extra["name"]: rb.sec_molal.reshape(-1, n)[i] for i, c in enumerate(b.complexes)})
+    for name, x in sa.items():
+        err = np.abs(sb[name] - x) / np.maximum(np.abs(x), 1e-300)
+        assert err.max() <= 1e-9, (name, err.max())
+    k_area = 1e-9 * ra.mnrl_area
+    assert (np.abs(rb.mnrl_rate - ra.mnrl_rate) / k_area).max() <= 5e-9
+    assert (np.abs(rb.mnrl_volfrac - ra.mnrl_volfrac) / ra.mnrl_volfrac).max() <= 1e-12

@@ -451,3 +451,17 @@ def test_error_statement_against_extended_precision(oracle, kind):
         d = rep["double_vs_extended"][q]
         assert e["max"] <= 1e-8, (q, e)
         assert e["p99"] <= 4 * d["p99"] + 1e-12, (q, e, d)
+
+
+def test_network_from_database_in_a_swapped_basis(oracle, tmp_path):
+    """A network read from a PFLOTRAN-format database with CO2(aq) primary
+    instead of HCO3- (basis swap) through the GPU library: parity with the
+    oracle in that basis at the usual bar."""
+    import kat
+    db, a, b = kat.calcite_networks_two_bases(tmp_path / "calcite.dat")
+    _, opt, ca, dt = workloads.calcite_cells(4096, seed=9, net=a)
+    ca.sec_molal = np.zeros(a.Nc * ca.ncells)
+    cb = kat.cells_in_basis(oracle, a, b, ca)
+    ref, gpu, _ = run_both(oracle, b, opt, cb, dt)
+    assert (ref.status == 0).all() and (gpu.status == 0).all()
+    assert_parity(b, gpu, ref)
