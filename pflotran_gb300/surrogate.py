@@ -9,8 +9,6 @@ from __future__ import annotations
 
 import time
 
-import numpy as np
-
 
 def generate(step, make_cells, n, seed, dt, chunk=2_097_152):
     """(X [M,16] float32, molal [N,M] float64) device tensors from `n` cells

@@ -1,6 +1,5 @@
 """Transport stand-in of the time-stepped run (CPU): permeability field,
 Darcy fluxes and upwind advection."""
-import numpy as np
 import pytest
 
 torch = pytest.importorskip("torch")

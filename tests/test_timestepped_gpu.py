@@ -4,7 +4,6 @@ sampled cells every step."""
 import json
 import os
 
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
