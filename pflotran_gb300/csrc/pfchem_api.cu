@@ -861,8 +861,13 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   add(cl->eqionx_ref_cation_sorbed_conc, std::max(n.Nix, 1));
   add(cl->srfcplxrxn_free_site_conc, std::max(n.Nsr, 1));
   for (auto &x : arrs) {
-    CUDA_TRY(c, cudaMalloc(&x.save, x.bytes));
-    CUDA_TRY(c, cudaMemcpyAsync(x.save, x.p, x.bytes, cudaMemcpyDeviceToDevice, c->stream));
+    cudaError_t ae = cudaMalloc(&x.save, x.bytes);
+    if (ae == cudaSuccess) ae = cudaMemcpyAsync(x.save, x.p, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+    if (ae != cudaSuccess) {  // release the backups made so far
+      for (auto &y : arrs)
+        if (y.save) cudaFree(y.save);
+      return fail(c, -2, "autotune state backup: %s", cudaGetErrorString(ae));
+    }
   }
   const int blocks[] = {32, 64, 128};
   const int refills[] = {1, 4, 8, 16, 32};
