@@ -1087,6 +1087,7 @@ int pfchem_surrogate_enable(pfchem_ctx *c, int on) {
 int64_t pfchem_surrogate_gradients(pfchem_ctx *c, const float *X, const double *molal, int64_t M, float *grad_host,
                                    float *loss_host) {
   if (!c || !X || !molal || !grad_host || !loss_host) return -1;
+  if (M < 1) return fail(c, -1, "no samples");
   cudaSetDevice(c->device);
   int e = need_surrogate(c, 1);
   if (e) return e;
