@@ -1633,6 +1633,8 @@ int pfo_equilibrate_constraints(const pfchem_network *net, const pfchem_options 
 int pfo_equilibrate_constraint(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
                                const int *type, const double *conc, int *iters) {
   Net w = make_net(net, opt);
+  for (int j = 0; j < w.N; ++j)
+    if (type[j] < kConTotal || type[j] >= kConMineral) return -1;  // mineral rows need the batch entry
   Cell<double> c;
   load_cell(w, cells, 0, c);
   update_temp_dependent_coefs(w, *opt, c);

@@ -176,3 +176,15 @@ def test_calcite_kinetics_volume_fractions_gold(oracle):
     for key in ("Total H+", "Total HCO3-", "Total Ca++"):
         assert abs(out[key] - gold[key]) <= 1e-11, (key, out[key], gold[key])
     assert abs(out["pH"] - gold["pH"]) <= 1e-9
+
+
+def test_single_cell_constraint_rejects_rows_it_cannot_take(oracle):
+    """The single-cell constraint entry has no mineral ids: a MINERAL or an
+    unknown row type is an error, not a read through a null table."""
+    fx = kat.load("kat_calcite_kinetics.json")
+    net = kat.build_network(fx, oracle)
+    from pflotran_gb300.network import default_options
+    b = kat.one_cell(net, fx, oracle)
+    for bad in ([1, 1, 6], [1, 0, 1], [7, 1, 1]):
+        with pytest.raises(RuntimeError):
+            oracle.equilibrate_constraint(net.as_struct(), default_options(use_isothermal=1), b, bad, [1e-5] * 3)
