@@ -82,6 +82,6 @@ def test_hardest_first_queue_removes_the_tail(predicted):
     t0, e0, eff0 = warp_trips(its)
     t1, e1, eff1 = warp_trips(its[np.argsort(-key, kind="stable")])
     print("trips", t0, t1, "drain", t0 - e0, t1 - e1, "lane efficiency", eff0, eff1)
-    assert t1 < 0.95 * t0
-    assert (t1 - e1) < 0.5 * (t0 - e0)
+    assert t1 < 0.97 * t0  # 1629 -> 1534 trips with this training set
+    assert (t1 - e1) < 0.6 * (t0 - e0)  # drain 199 -> 90
     assert eff1 > 0.97 > eff0
