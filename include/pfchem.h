@@ -167,7 +167,19 @@ typedef struct pfchem_options {
   double max_residual_tolerance;      /* reaction%max_residual_tolerance (1e-12) */
   int32_t update_kinetic_state;       /* 1: fuse RUpdateKineticState after the solve */
   int32_t jacobian;                   /* PFCHEM_JACOBIAN_* (0 = the reference's) */
+  int32_t exact_jacobian_after;       /* 0: never; K > 0: see below */
+  int32_t reserved3;                  /* 0 */
 } pfchem_options;
+/* exact_jacobian_after = K > 0: a cell still unconverged after K Newton
+ * iterations continues with the EXACT Jacobian and without RReact's x0.1
+ * damping.  RReact damps every update after iteration 50 and loops until
+ * converged (reaction.F90:3478-3496; its "> 500" stop is unreachable), so a
+ * cell whose reference-Jacobian Newton converges slowly crawls for hundreds
+ * of iterations (on the synthetic 12-species workload 2 % of cells pass 50
+ * iterations; uncapped they need a median 377 and up to ~2200).  With K = 50
+ * the first 50 iterations are RReact's and such cells converge 2-4 iterations
+ * later to the same root (same residual, same relative-residual test).
+ * 0 reproduces RReact's damped path, cut at max_iterations. */
 /* Newton Jacobian.  REFERENCE forms it as RReact does, with three
  * inexact terms that make Newton converge linearly:
  *  - RTotalSorbEqSurfCplx1 adds the free-site part of dS_k/dm_j only for the

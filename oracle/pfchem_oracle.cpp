@@ -911,7 +911,9 @@ int newton_system(const Net &w, const pfchem_options &o, Cell<R> &c, const R *fi
 // given, is a second starting guess (the learned warm start): the residual
 // is evaluated at both guesses and Newton starts from `alt` when its norm is
 // no larger, keeping the ion-exchange warm start of the evaluation it chose
-// and the surface free-site state it was given.
+// and the surface free-site state it was given.  With the library option
+// exact_jacobian_after = K > 0 (no counterpart in the reference) iterations
+// past K use the exact Jacobian and skip the damping of :3478-3496.
 template <class R>
 int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, R dt, R I_start,
            int *num_iterations_out, const double *alt = nullptr, bool *alt_used = nullptr) {
@@ -960,15 +962,20 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
   }
   int status = PFCHEM_CELL_CONVERGED;
   R residual[P], J[P][P], update[P], prev_solution[P], new_solution[P];
+  // exact_jacobian_after = K > 0: past iteration K the exact Jacobian, no damping
+  Net w_exact = w;
+  w_exact.exact_jac = true;
   for (;;) {
     ++num_iterations;
+    const bool rescue = o.exact_jacobian_after > 0 && num_iterations > o.exact_jacobian_after;
+    const Net &wn = rescue ? w_exact : w;
     if (o.act_coef_update_frequency == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) {
       if (activity_coefficients(w, o, c, num_iterations == 1, I_start)) {
         status = PFCHEM_CELL_INNER_MAXITER;
         break;
       }
     }
-    if (newton_system(w, o, c, fixed_accum, psv_t, dt, residual, J)) {
+    if (newton_system(wn, o, c, fixed_accum, psv_t, dt, residual, J)) {
       status = PFCHEM_CELL_INNER_MAXITER;
       break;
     }
@@ -1032,7 +1039,7 @@ int rreact(const Net &w, const pfchem_options &o, Cell<R> &c, const R *tran_xx, 
     if (o.max_relative_change_tolerance > 0 &&
         maximum_relative_change < R(o.max_relative_change_tolerance))
       break;
-    if (num_iterations > 50) {
+    if (num_iterations > 50 && !rescue) {
       R scale = R(0.1);  // reaction.F90:3478-3496: only the first branch is reachable
       for (int j = 0; j < N; ++j) new_solution[j] = scale * (new_solution[j] - prev_solution[j]) + prev_solution[j];
     }

@@ -90,6 +90,7 @@ class Options(C.Structure):
         ("max_dlnC", C.c_double), ("max_relative_change_tolerance", C.c_double),
         ("max_residual_tolerance", C.c_double),
         ("update_kinetic_state", C.c_int32), ("jacobian", C.c_int32),
+        ("exact_jacobian_after", C.c_int32), ("reserved3", C.c_int32),
     ]
 
 

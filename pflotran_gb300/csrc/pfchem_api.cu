@@ -155,6 +155,8 @@ int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o
   if (o->jacobian != PFCHEM_JACOBIAN_REFERENCE && o->jacobian != PFCHEM_JACOBIAN_EXACT)
     return fail(c, -1, "unknown jacobian %d", o->jacobian);
   n.jac_exact = o->jacobian == PFCHEM_JACOBIAN_EXACT;
+  if (o->exact_jacobian_after < 0) return fail(c, -1, "exact_jacobian_after must be >= 0");
+  n.exact_after = o->exact_jacobian_after;
   n.max_dlnC = o->max_dlnC;
   n.rel_change_tol = o->max_relative_change_tolerance;
   n.res_tol = o->max_residual_tolerance;

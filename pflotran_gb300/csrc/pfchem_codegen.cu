@@ -133,6 +133,10 @@ struct Gen {
     return e;
   }
   bool act() const { return n.act_freq != PFCHEM_ACT_COEF_FREQUENCY_OFF; }
+  // exact_jacobian_after: the Jacobian's exact terms are selected at run time
+  bool rescue() const { return n.exact_after > 0 && !n.jac_exact; }
+  // the exact-Jacobian condition as a C expression ("exact" at run time)
+  std::string EX() const { return n.jac_exact ? "true" : (rescue() ? "exact" : "false"); }
   bool any_h2o() const {
     for (int i = 0; i < n.Nc; ++i)
       if (n.ch2o[i] != 0.0) return true;
@@ -291,7 +295,8 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   // Residual (and with jac the Jacobian d/dln m into [J | .]) at L.m
   void evaluate(bool jac) {
     const int N = n.N;
-    o << "__device__ __forceinline__ int evaluate_" << (jac ? "jac" : "res") << "(Lane &L, double *Jb) {\n";
+    o << "__device__ __forceinline__ int evaluate_" << (jac ? "jac" : "res") << "(Lane &L, double *Jb"
+      << (jac && rescue() ? ", bool exact" : "") << ") {\n";
     o << "  int status = 0;\n";
     if (prod_any()) {
       bool neg[PFCHEM_MAX_PRI] = {};
@@ -531,25 +536,29 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         }
         if (jac) {
           o << "  { const double nuS = " << times(n.sfs[k], "S" + I(q)) << " * ifree;\n";
-          if (n.jac_exact) {
-            // the free site couples every component on the site
-            for (int j : site_comps) {
-              double nu = 0.0;
-              for (int l = 0; l < n.sn[k]; ++l)
-                if (n.sid[k][l] == j) nu += n.snu[k][l];
-              o << "    { const double t = (" << (nu != 0.0 ? times(nu, "S" + I(q)) + " + " : "") << "nuS * dSx" << j
-                << " * iden) * L.v_t;\n";
+          // terms of the complex's own components (RReact's Jacobian) ...
+          for (int l = 0; l < n.sn[k]; ++l) {
+            const int j = n.sid[k][l];
+            o << "    { const double t = (" << times(n.snu[k][l], "S" + I(q)) << " + nuS * dSx" << j
+              << " * iden) * L.v_t;\n";
+            for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
+            o << "    }\n";
+          }
+          // ... and, exact, the free site's coupling to the site's other components
+          std::vector<int> others;
+          for (int j : site_comps) {
+            bool own = false;
+            for (int l = 0; l < n.sn[k]; ++l) own |= n.sid[k][l] == j;
+            if (!own) others.push_back(j);
+          }
+          if (!others.empty() && EX() != "false") {
+            o << "    if (" << EX() << ") {\n";
+            for (int j : others) {
+              o << "    { const double t = (nuS * dSx" << j << " * iden) * L.v_t;\n";
               for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
               o << "    }\n";
             }
-          } else {
-            for (int l = 0; l < n.sn[k]; ++l) {
-              const int j = n.sid[k][l];
-              o << "    { const double t = (" << times(n.snu[k][l], "S" + I(q)) << " + nuS * dSx" << j
-                << " * iden) * L.v_t;\n";
-              for (int p = 0; p < n.sn[k]; ++p) acc(o, "  " + J(n.sid[k][p], j), n.snu[k][p], "t");
-              o << "    }\n";
-            }
+            o << "    }\n";
           }
           o << "  }\n";
         }
@@ -604,12 +613,18 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       }
       if (jac) {
         // exact Jacobian: signed affinity, no den/1000 factor, nothing where QK is capped
-        if (n.jac_exact) o << "  if " << qk_ok << " {\n";
-        if (n.has_affpow)
-          o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << (n.jac_exact ? " / aff;\n" : " / fabs(aff);\n");
-        else o << "  double dIm_dQK = -(Imc * L.vol) * kr;\n";
+        const std::string ex = EX();
+        if (ex == "true") o << "  if " << qk_ok << " {\n";
+        else if (ex != "false") o << "  if (!" << ex << " || " << qk_ok << ") {\n";
+        if (n.has_affpow) {
+          if (ex == "true") o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << " / aff;\n";
+          else if (ex == "false") o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << " / fabs(aff);\n";
+          else o << "  double dIm_dQK = -ImV * " << lit(n.mpow[mm]) << " / (" << ex << " ? aff : fabs(aff));\n";
+        } else o << "  double dIm_dQK = -(Imc * L.vol) * kr;\n";
         if (gen_aff) o << "  dIm_dQK = dIm_dQK * " << lit(1.0 / sig) << " / QK * (1.0 - aff);\n";
-        o << (n.jac_exact ? "  double gq = dIm_dQK * QK;\n" : "  double gq = dIm_dQK * QK * L.den_L;\n");
+        if (ex == "true") o << "  double gq = dIm_dQK * QK;\n";
+        else if (ex == "false") o << "  double gq = dIm_dQK * QK * L.den_L;\n";
+        else o << "  double gq = dIm_dQK * QK * (" << ex << " ? 1.0 : L.den_L);\n";
         if (n.mlim[mm] > 0.0) {
           o << "  { const double d2 = 1.0 + (1.0 - aff) * " << lit(1.0 / n.mlim[mm]) << ";\n";
           o << "    gq = gq * (1.0 + QK * " << lit(1.0 / n.mlim[mm]) << " / d2) / d2; }\n";
@@ -620,7 +635,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
           for (int k = 0; k < nz; ++k) acc(o, "  " + J(n.mid[mm][k], j), n.mnu[mm][k], "t");
           o << "  }\n";
         }
-        if (n.jac_exact) o << "  }\n";
+        if (ex != "false") o << "  }\n";
       }
       o << "  }\n  }\n";
     }
@@ -764,7 +779,13 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       activity("Iv");
       o << "  }\n";
     }
-    o << "  int st = evaluate_jac(L, Jb); if (st) return st;\n";
+    if (rescue()) {
+      // past exact_jacobian_after iterations: the exact Jacobian, no damping
+      o << "  const bool rescue = L.iter > " << n.exact_after << ";\n";
+      o << "  int st = evaluate_jac(L, Jb, rescue); if (st) return st;\n";
+    } else {
+      o << "  int st = evaluate_jac(L, Jb); if (st) return st;\n";
+    }
     o << "  bool bad; const bool conv = converged(L, &bad);\n";
     o << "  if (bad) return " << PFCHEM_CELL_NONFINITE << ";\n";
     o << "  if (conv) return " << PFCHEM_CELL_CONVERGED << ";\n";
@@ -807,7 +828,10 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     }
     o << "  if (nf) return " << PFCHEM_CELL_NONFINITE << ";\n";
     if (n.rel_change_tol > 0.0) o << "  if (mrc < " << lit(n.rel_change_tol) << ") return " << PFCHEM_CELL_CONVERGED << ";\n";
-    o << "  if (L.iter > 50) {\n";
+    if (n.exact_after > 0)
+      o << "  if (L.iter > 50 && L.iter <= " << n.exact_after << ") {\n";
+    else
+      o << "  if (L.iter > 50) {\n";
     for (int j = 0; j < N; ++j)
       o << "    mnew[" << j << "] = 0.1 * (mnew[" << j << "] - L.m[" << j << "]) + L.m[" << j << "]; L.m[" << j
         << "] = mnew[" << j << "]; L.lm[" << j << "] = log(mnew[" << j << "]);\n";

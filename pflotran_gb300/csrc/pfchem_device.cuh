@@ -25,6 +25,7 @@ struct DevNet {
   int32_t use_log, act_freq, use_h2o, isothermal, resid_kind, accum_mode, max_iter, update_kin;
   int32_t has_temkin, has_minscale, has_affpow, has_h2o_rxn;
   int32_t jac_exact;  // PFCHEM_JACOBIAN_EXACT
+  int32_t exact_after;  // exact_jacobian_after (0: never)
   double max_dlnC, rel_change_tol, res_tol;
   double A, B, Bdot;
   // primaries

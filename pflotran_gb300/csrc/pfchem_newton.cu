@@ -171,7 +171,7 @@ __device__ void setup(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> 
 // the lane's current m.  Returns 0, or a non-converged status when an inner
 // loop hit its cap.
 template <class S, bool JAC>
-__device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
+__device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js, bool exact) {
   const int N = n.N;
   double lna[S::NP], absP[S::NP], absS[S::NP];
   for (int j = 0; j < N; ++j) {
@@ -344,7 +344,7 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
         L.S_[i] += v;
         absS[i] += fabs(v);
       }
-      if (JAC && n.jac_exact) {
+      if (JAC && exact) {
         // the free site couples every component on the site
         double t[S::NP];
         for (int j = 0; j < N; ++j) t[j] = nuS * dSx[j] * iden;
@@ -395,11 +395,11 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js) {
       L.F[i] += v;
       L.Sc[i] += fabs(v);
     }
-    if (JAC && !(n.jac_exact && lnQK > 6.90776)) {  // exact: a capped QK does not depend on m
-      double dIm_dQK = n.has_affpow ? -ImV * n.mpow[mm] / (n.jac_exact ? aff : fabs(aff)) : -(Imc * L.vol) * kr;
+    if (JAC && !(exact && lnQK > 6.90776)) {  // exact: a capped QK does not depend on m
+      double dIm_dQK = n.has_affpow ? -ImV * n.mpow[mm] / (exact ? aff : fabs(aff)) : -(Imc * L.vol) * kr;
       if (n.has_temkin || n.has_minscale) dIm_dQK = dIm_dQK * (1.0 / sig) / QK * (1.0 - aff);
       // d/dln m_j of QK is nu_j QK; the reference scales it by den*1e-3
-      double g = dIm_dQK * QK * (n.jac_exact ? 1.0 : L.den_mnrl) * L.jac_mnrl;
+      double g = dIm_dQK * QK * (exact ? 1.0 : L.den_mnrl) * L.jac_mnrl;
       if (n.mlim[mm] > 0.0) {
         const double d2 = 1.0 + (1.0 - aff) / n.mlim[mm];
         g = g * (1.0 + QK / n.mlim[mm] / d2) / d2;
@@ -516,7 +516,9 @@ __device__ int newton_step(const DevNet &n, Lane<S> &L, double *J, int js) {
     I *= 0.5;
     activity(n, L, I);
   }
-  int st = evaluate<S, true>(n, L, J, js);
+  // past exact_jacobian_after iterations: the exact Jacobian, no damping
+  const bool rescue = n.exact_after > 0 && L.iter > n.exact_after;
+  int st = evaluate<S, true>(n, L, J, js, n.jac_exact || rescue);
   if (st) return st;
   bool bad;
   double rn;
@@ -566,7 +568,7 @@ __device__ int newton_step(const DevNet &n, Lane<S> &L, double *J, int js) {
   }
   if (nf) return PFCHEM_CELL_NONFINITE;
   if (n.rel_change_tol > 0.0 && mrc < n.rel_change_tol) return PFCHEM_CELL_CONVERGED;
-  if (L.iter > 50) {
+  if (L.iter > 50 && !rescue) {
     // reaction.F90:3478-3496 (only the 0.1 branch is reachable)
     for (int j = 0; j < N; ++j) {
       mnew[j] = 0.1 * (mnew[j] - L.m[j]) + L.m[j];
@@ -630,7 +632,7 @@ __device__ void finalize(const DevNet &n, const CellArgs &a, int64_t cell, Lane<
 // plain guess (the fallback reference).
 template <class S>
 __device__ void arm_alt_guess(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> &L) {
-  evaluate<S, false>(n, L, nullptr, 0);
+  evaluate<S, false>(n, L, nullptr, 0, n.jac_exact);
   bool bad;
   double rn;
   converged(n, L, &bad, &rn);
@@ -834,7 +836,7 @@ __global__ void __launch_bounds__(256) kinetic_state_kernel(const __grid_constan
   if (a.active && a.active[cell] <= 0) return;
   Lane<S> L;
   setup(n, a, cell, L, 1.0 / a.dt);
-  evaluate<S, false>(n, L, nullptr, 0);
+  evaluate<S, false>(n, L, nullptr, 0, n.jac_exact);
   const int64_t nc = a.ncells;
   for (int k = 0; k < n.Nm; ++k) {
     if (a.rate) a.rate[k * nc + cell] = L.rate[k];
@@ -893,7 +895,7 @@ __global__ void __launch_bounds__(32) reaction_blocks_kernel(const __grid_consta
   L.jac_aq = L.den_L;
   L.v_t = 0.0;
   L.jac_mnrl = 0.0;
-  status |= evaluate<S, true>(n, L, J, js);
+  status |= evaluate<S, true>(n, L, J, js, n.jac_exact);
   if (o.total)
     for (int j = 0; j < N; ++j) o.total[j * nc + cell] = L.Psi[j] * L.den_L;
   if (o.dtotal) store_block(n, L, J, js, o.dtotal, cell);
@@ -901,7 +903,7 @@ __global__ void __launch_bounds__(32) reaction_blocks_kernel(const __grid_consta
   if (n.Nix + n.Nsr > 0 && (o.total_sorb || o.dtotal_sorb)) {
     L.jac_aq = 0.0;
     L.v_t = 1.0;
-    status |= evaluate<S, true>(n, L, J, js);
+    status |= evaluate<S, true>(n, L, J, js, n.jac_exact);
     if (o.total_sorb)
       for (int j = 0; j < N; ++j) o.total_sorb[j * nc + cell] = L.S_[j];
     if (o.dtotal_sorb) store_block(n, L, J, js, o.dtotal_sorb, cell);
@@ -915,7 +917,7 @@ __global__ void __launch_bounds__(32) reaction_blocks_kernel(const __grid_consta
   L.jac_aq = 0.0;
   L.v_t = 0.0;
   L.jac_mnrl = 1.0;
-  status |= evaluate<S, true>(n, L, J, js);
+  status |= evaluate<S, true>(n, L, J, js, n.jac_exact);
   for (int j = 0; j < N; ++j) o.res[j * nc + cell] = L.F[j];
   store_block(n, L, J, js, o.jac, cell);
   for (int k = 0; k < n.Nm; ++k)
@@ -1008,7 +1010,7 @@ __global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ 
       for (int i = 0; i < n.Nc; ++i) I += n.cZ2[i] * L.C[i];
       activity(n, L, 0.5 * I);
     }
-    if (evaluate<S, true>(n, L, J, js)) {
+    if (evaluate<S, true>(n, L, J, js, n.jac_exact)) {
       status = 1;
       break;
     }
@@ -1115,7 +1117,7 @@ __global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ 
   // totals and sorption at the final free ions with the last activity
   // coefficients (what the next step's RTAuxVarCompute sees)
   for (int j = 0; j < N; ++j) L.lnm[j] = log(L.m[j]);
-  if (status == 0 && evaluate<S, true>(n, L, J, js)) status = 1;
+  if (status == 0 && evaluate<S, true>(n, L, J, js, n.jac_exact)) status = 1;
   double I = 0.0;
   for (int j = 0; j < N; ++j) {
     a.pri_molal[j * nc + cell] = L.m[j];

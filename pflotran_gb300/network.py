@@ -289,6 +289,9 @@ def default_options(**kw) -> abi.Options:
     o.max_residual_tolerance = 1e-12
     o.update_kinetic_state = 1
     o.jacobian = abi.JACOBIAN_REFERENCE
+    # RReact's own iterations up to its damping threshold (iteration 50), the
+    # exact Jacobian without damping for the few cells still unconverged
+    o.exact_jacobian_after = 50
     for k, v in kw.items():
         setattr(o, k, v)
     return o

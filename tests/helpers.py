@@ -1,25 +1,9 @@
 """Shared helpers of the parity tests: workloads, scales and comparisons."""
 import numpy as np
 
+from oracle.parity import (cell_errors, error_statement, per_cell_bar, rel_err, total_scale,  # noqa: F401
+                           truth_options)
 from pflotran_gb300 import abi
-from pflotran_gb300.workloads import Speciator
-
-
-def total_scale(net, cells):
-    """Per-component magnitude of the aqueous total: den_L*(m_j + sum_i |nu_ij| C_i)."""
-    nu = Speciator(net).nu_np
-    n = cells.ncells
-    m = cells.pri_molal.reshape(net.N, n)
-    if net.Nc:
-        C = cells.sec_molal.reshape(-1, n)[:net.Nc]
-        s = m + np.abs(nu).T @ C
-    else:
-        s = m.copy()
-    return s * (cells.den_kg * 1e-3)[None, :]
-
-
-def rel_err(x, y, scale):
-    return np.abs(x - y) / np.maximum(np.abs(y), scale)
 
 
 def compare(net, gpu, ref, tol=1e-10, mask=None):
@@ -34,8 +18,7 @@ def compare(net, gpu, ref, tol=1e-10, mask=None):
     if net.Nm:
         k = np.array([mn.extra["k"] for mn in net.minerals])[:, None]
         area = ref.mnrl_area.reshape(-1, n)[:net.Nm]
-        rs = k * area * 1e-12 + 1e-300  # scale: rate constant x area (x 1e-12 below which rates are noise)
-        rs = k * area
+        rs = k * area  # scale: rate constant x area
         out["mnrl_rate"] = rel_err(gpu.mnrl_rate.reshape(-1, n)[:net.Nm], ref.mnrl_rate.reshape(-1, n)[:net.Nm],
                                    rs)[:, mask].max()
         out["mnrl_volfrac"] = rel_err(gpu.mnrl_volfrac.reshape(-1, n)[:net.Nm],
@@ -80,24 +63,7 @@ def constraint_problem(oracle, net, opt, cells, rows):
     return types, minerals, np.ascontiguousarray(values)
 
 
-def cell_errors(net, x, y):
-    """Per-cell scaled relative errors of x against y (max over the
-    components) for the aqueous totals, mineral volume fractions and mineral
-    rates, with the scales of `compare`."""
-    n = y.ncells
-    errs = {"total": rel_err(x.total_out.reshape(net.N, n), y.total_out.reshape(net.N, n), total_scale(net, y))}
-    if net.Nm:
-        k = np.array([mn.extra["k"] for mn in net.minerals])[:, None]
-        area = y.mnrl_area.reshape(-1, n)[:net.Nm]
-        errs["mnrl_rate"] = rel_err(x.mnrl_rate.reshape(-1, n)[:net.Nm], y.mnrl_rate.reshape(-1, n)[:net.Nm], k * area)
-        errs["mnrl_volfrac"] = rel_err(x.mnrl_volfrac.reshape(-1, n)[:net.Nm], y.mnrl_volfrac.reshape(-1, n)[:net.Nm],
-                                       1e-300)
-    return {q: e.max(axis=0) for q, e in errs.items()}
-
-
-def error_statement(net, x, y, mask=None):
-    """Max and 99th percentile over the cells in `mask` of `cell_errors`."""
-    errs = cell_errors(net, x, y)
-    if mask is None:
-        mask = np.ones(y.ncells, bool)
-    return {q: {"max": float(e[mask].max()), "p99": float(np.percentile(e[mask], 99))} for q, e in errs.items()}
+def truth_solve(oracle, net, opt, cells, dt, start, nthreads=None):
+    """The root of the cells' equations (see oracle.parity.truth_solve)."""
+    from oracle import parity
+    return parity.truth_solve(net, opt, dt, cells, start, nthreads)
