@@ -6,15 +6,32 @@ kinetic TST minerals, 4 ion-exchange and 2 surface-complexation reactions)
 on 2,097,152 cells, FP64, dt = 1 day, converged to a 1e-12 relative
 residual.  One "step" is one reaction step over all cells.
 
-  value   converged cell solves/s with inputs resident in HBM (device time of
-          the solve, CUDA events on the library's stream, summed over the
-          timed steps; the cell state is restored from a pristine copy between
-          steps, outside the timed interval)
+  value   CONVERGED cell solves/s with the learned warm start, inputs
+          resident in HBM (cells whose status is not CONVERGED are not
+          counted; device time of the step graph, CUDA events on the
+          library's stream, summed over the timed steps; the cell state is
+          restored from a pristine copy between steps, outside the timed
+          interval).  warm_start.plain_value is the same for the plain
+          previous-step guess.
   e2e     the same metric through pfchem_react_batch with pinned host
           buffers: every step uploads inputs and state and downloads state
           and outputs
-  cpu_baseline  the oracle (C++ restatement of RReact) on a bounded sample
-          of the same cells on all host cores
+  cpu_baseline  the oracle (C++ restatement of RReact) on a seeded random
+          sample of the same cells on all host cores; also 1 core and the
+          literal RReact accumulation
+  parity  GPU against the oracle on that sample, for the plain and the
+          warm-started step: max / p99 scaled relative errors of totals,
+          mineral rates and volume fractions, and the per-cell bar (within
+          1e-10 of the oracle, or no farther than it from the root of the
+          equations, a long-double solve to a 1e-12-tighter residual)
+  reference_path  the same plain step with exact_jacobian_after = 0
+          (RReact's damped iteration, cut at 200 iterations): its converged
+          solves/s, and how far its capped cells are from RReact run
+          without a cap
+  calcite_grid  the calcite network on 100^3 cells, temperature-dependent
+          log K, plain Newton, graph-captured
+  timestepped   128^3 cells x 50 steps of transport + reaction, one CUDA graph
+          per step, drift against the oracle on sampled cells
 
 `--impl reference` times the reference's CPU implementation of the step
 (the oracle port: PFLOTRAN's Fortran cannot be built in this image) on the
@@ -39,6 +56,7 @@ NCELLS = 2_097_152
 # DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
 # on 524,288 cells of the same workload (561.5 MB read + 290.3 MB written)
 TRAFFIC_BYTES_PER_CELL = (561539840 + 290312704) / 524288
+SAMPLE_SEED = 12345
 
 
 def parse():
@@ -50,12 +68,17 @@ def parse():
     p.add_argument("--ncells", type=int, default=NCELLS)
     p.add_argument("--cpu-sample", type=int, default=20000)
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--autotune", action="store_true")
+    p.add_argument("--autotune", action=argparse.BooleanOptionalAction, default=True,
+                   help="choose the launch with pfchem_autotune on a 262,144-cell draw of the workload")
     p.add_argument("--train-samples", type=int, default=8_388_608)
     p.add_argument("--epochs", type=int, default=12)
     p.add_argument("--plain-only", action="store_true")
     p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
                    help="also time the step with the exact Newton Jacobian")
+    p.add_argument("--reference-path", action=argparse.BooleanOptionalAction, default=True,
+                   help="also time the plain step with exact_jacobian_after = 0")
+    p.add_argument("--calcite-grid", action=argparse.BooleanOptionalAction, default=True)
+    p.add_argument("--timestepped", action=argparse.BooleanOptionalAction, default=True)
     p.add_argument("--jacobian", choices=("reference", "exact"), default="reference",
                    help="Newton Jacobian of the headline run")
     return p.parse_args()
@@ -115,28 +138,83 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def make_workload(ncells, device="cpu", rank=0):
+def make_workload(ncells, device="cpu", rank=0, seed=2024):
     """The synthetic 12-species workload; rank r of a multi-GPU run takes its
     own seeded shard of cells (weak scaling, no data exchange)."""
     from pflotran_gb300 import workloads
     net = workloads.synthetic_network()
-    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=2024 + 7919 * rank, net=net, device=device)
+    net, opt, cells, dt = workloads.synthetic_cells(ncells, seed=seed + 7919 * rank, net=net, device=device)
     return net, opt, cells, dt
 
 
+def sample_indices(n, k, seed=SAMPLE_SEED):
+    """A seeded random sample of k of the n cells (sorted)."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n, min(k, n), replace=False))
+
+
+def _opts(opt, **kw):
+    from pflotran_gb300 import abi
+    o = abi.Options.from_buffer_copy(opt)
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
 def cpu_baseline(net, opt, cells, dt, sample):
-    from oracle import oracle
-    idx = np.arange(min(sample, cells.ncells))
+    """The oracle on a seeded random sample of the workload: all host cores
+    (the reported baseline), one core on a tenth of the sample, and the
+    literal RReact accumulation (accum_scale = 1, absolute residual and
+    relative-change tests).  Returns (baseline dict, sample indices, the
+    sample's inputs, the oracle's all-core solution)."""
+    from oracle import parity
+    idx = sample_indices(cells.ncells, sample)
     sub = cells.subset(idx, net)
-    sub.iterations = np.zeros(len(idx), np.int32)
-    sub.status = np.zeros(len(idx), np.int32)
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
-    oracle.react(net.as_struct(), opt, dt, sub, 0, threads)
+    ref = parity.solve(net, opt, dt, sub, 0, threads)
     el = time.perf_counter() - t0
-    return {"value": len(idx) / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"first {len(idx)} cells of the {cells.ncells}-cell workload, oracle RReact in double, "
-                      f"{threads} std::threads"}, sub
+    one = sub.subset(np.arange(max(1, len(idx) // 10)), net)
+    t0 = time.perf_counter()
+    r1 = parity.solve(net, opt, dt, one, 0, 1)
+    el1 = time.perf_counter() - t0
+    # RReact's literal residual is not divided by dt while its Jacobian is
+    # (reaction.F90:3424-3426 vs :5189-5190): its Newton step is dt times too
+    # long, so the literal form is timed at dt = 1 s, where the two agree
+    lit_opt = _opts(opt, accum_mode=1, residual_tol_kind=0, max_relative_change_tolerance=1e-6)
+    t0 = time.perf_counter()
+    lit = parity.solve(net, lit_opt, 1.0, sub, 0, threads)
+    el_lit = time.perf_counter() - t0
+    conv = int((ref.status == 0).sum())
+    cb = {"value": conv / el, "unit": UNIT, "cores": threads, "kind": "port",
+          "sample": f"{len(idx)} cells drawn at random (seed {SAMPLE_SEED}) from the {cells.ncells}-cell workload, "
+                    f"oracle RReact in double, {threads} std::threads; converged cells counted",
+          "converged": conv,
+          "one_core": {"value": int((r1.status == 0).sum()) / el1, "unit": UNIT, "cells": one.ncells},
+          "literal_rreact": {"value": int((lit.status == 0).sum()) / el_lit, "unit": UNIT, "cores": threads,
+                             "converged": int((lit.status == 0).sum()), "cells": len(idx),
+                             "options": "accum_scale 1 (RReact's residual without /dt), absolute 1e-12 residual, "
+                                        "1e-6 relative-change exit, dt 1 s"}}
+    return cb, idx, sub, ref
+
+
+def parity_block(net, opt, dt, sub, ref, gpu_sub, truth, alt_guess=None):
+    """GPU against the oracle on the sample: error statement and the per-cell
+    bar against the root."""
+    from oracle import parity
+    both = (ref.status == 0) & (gpu_sub.status == 0)
+    st = parity.error_statement(net, gpu_sub, ref, both)
+    bar = parity.per_cell_bar(net, gpu_sub, ref, truth, 1e-10, both & (truth.status == 0))
+    out = {"cells": int(both.sum()), "gpu_nonconverged": int((gpu_sub.status != 0).sum()),
+           "oracle_nonconverged": int((ref.status != 0).sum()),
+           "same_iterations": float(np.mean(ref.iterations[both] == gpu_sub.iterations[both])) if both.any() else None}
+    for q, e in st.items():
+        ok, exr, ext, ert = bar[q]
+        m = both & (truth.status == 0)
+        out[q] = dict(e, beyond_1e10=int((exr[both] > 1e-10).sum()), bar_failures=int((~ok).sum()),
+                      gpu_vs_root_max=float(ext[m].max()) if m.any() else None,
+                      oracle_vs_root_max=float(ert[m].max()) if m.any() else None)
+    return out
 
 
 def _cuda():
@@ -152,19 +230,20 @@ def run_reference(args):
     if rank != 0:
         return
     net, opt, cells, dt = make_workload(args.ncells, device="cuda" if _cuda() else "cpu")
-    from oracle import oracle
+    from oracle import parity
     threads = os.cpu_count() or 1
-    n = min(args.cpu_sample, cells.ncells)
-    sub0 = cells.subset(np.arange(n), net)
-    times = []
+    idx = sample_indices(cells.ncells, args.cpu_sample)
+    sub0 = cells.subset(idx, net)
+    n = len(idx)
+    times, conv = [], []
     for s in range(args.warmup + args.steps):
-        sub = sub0.copy()
         t0 = time.perf_counter()
-        oracle.react(net.as_struct(), opt, dt, sub, 0, threads)
+        r = parity.solve(net, opt, dt, sub0, 0, threads)
         el = time.perf_counter() - t0
         if s >= args.warmup:
             times.append(el)
-    value = n / (sum(times) / len(times))
+            conv.append(int((r.status == 0).sum()))
+    value = float(np.mean(conv)) / (sum(times) / len(times))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
@@ -173,11 +252,78 @@ def run_reference(args):
                                f"2 surface-complexation), {args.ncells} cells, dt 1 day, 1e-12 rel. residual",
                    "sample_cells_per_step": n},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": f"{n} of {args.ncells} cells per step (oracle C++ restatement of RReact; "
-                                   f"PFLOTRAN's Fortran cannot be compiled in this image)"},
+                         "sample": f"{n} of {args.ncells} cells per step, drawn at random (seed {SAMPLE_SEED}); "
+                                   f"oracle C++ restatement of RReact; PFLOTRAN's Fortran cannot be compiled in "
+                                   f"this image; converged cells counted"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def calcite_grid(args, local):
+    """Config 2: the calcite network on 100^3 cells with temperature-dependent
+    log K, plain Newton from the previous-step guess, graph-captured."""
+    import torch
+    from oracle import parity
+    from pflotran_gb300 import workloads
+    from pflotran_gb300.lib import ReactionStep
+    net, opt, host, dt = workloads.calcite_cells(1_000_000, seed=2, temperature_dependent=True,
+                                                 device=f"cuda:{local}")
+    step = ReactionStep(net, opt, device=local)
+    pristine = host.to_device()
+    dev = pristine.copy()
+    ms, conv, its = [], [], []
+    for s in range(args.warmup + args.steps):
+        for f in ("pri_molal", "ionic_strength", "mnrl_volfrac"):
+            getattr(dev, f).copy_(getattr(pristine, f))
+        torch.cuda.synchronize()
+        step.react(dev, dt)
+        st = step.stats()
+        if s >= args.warmup:
+            ms.append(st.kernel_ms)
+            conv.append(st.ncells - st.nonconverged)
+            its.append(st.sum_iterations / st.ncells)
+    g = dev.to_host()
+    idx = sample_indices(host.ncells, 20000, SAMPLE_SEED + 1)
+    sub = host.subset(idx, net)
+    ref = parity.solve(net, opt, dt, sub, 0)
+    gsub = g.subset(idx, net)
+    both = (ref.status == 0) & (gsub.status == 0)
+    return {"workload": "calcite network (3 primaries, 5 complexes, kinetic calcite), 1,000,000 cells, T in "
+                        "[10, 60] C with log K linear in T, dt 1 day, plain Newton, graph-captured",
+            "value": float(np.sum(conv)) / (float(np.sum(ms)) * 1e-3), "unit": UNIT,
+            "ms_per_step": float(np.mean(ms)), "mean_newton_iterations": float(np.mean(its)),
+            "nonconverged": int(host.ncells - conv[-1]),
+            "parity": {"cells": int(both.sum()), **parity.error_statement(net, gsub, ref, both)}}
+
+
+def timestepped(args, local):
+    """Config 5: 128^3 cells x 50 steps, upwind transport + reaction step in
+    one CUDA graph per step, learned warm start, drift against the oracle on
+    512 sampled cells per step."""
+    from oracle import oracle
+    from pflotran_gb300.os_run import OperatorSplitRun
+    run = OperatorSplitRun(shape=(128, 128, 128), warm_start=True, autotune=False, drift_sample=512, log=None,
+                           device=f"cuda:{local}")
+    fn = lambda n_, o_, dt_, c_: oracle.react(n_, o_, dt_, c_, 0, os.cpu_count() or 1)
+    recs = run.run(steps=50, oracle_fn=fn)
+    react = [r["solves_per_s"] for r in recs if "solves_per_s" in r]
+    worst = {k: max(r["drift"].get(k, 0.0) for r in recs) for k in ("pri_molal", "total", "mnrl_rate",
+                                                                       "mnrl_volfrac")}
+    return {"workload": "128^3 cells of the synthetic 12-species network, 50 steps of 1 day, upwind transport "
+                        f"({run.nsub} sub-steps) + reaction step with the learned warm start, one CUDA graph per step",
+            "steps": len(recs),
+            "reaction_solves_per_s_mean": float(np.mean(react)) if react else None,
+            "reaction_solves_per_s_first_last": [react[0], react[-1]] if react else None,
+            "step_solves_per_s_mean": float(np.mean([r["step_solves_per_s"] for r in recs])),
+            "transport_ms_mean": float(np.mean([r["transport_ms"] for r in recs if "transport_ms" in r]))
+            if react else None,
+            "mean_newton_iterations_first_last": [recs[0]["mean_iterations"], recs[-1]["mean_iterations"]],
+            "nonconverged_max": int(max(r["nonconverged"] for r in recs)),
+            "warm_start_used_frac_first_last": [recs[0]["warm_start_used"] / run.n,
+                                                recs[-1]["warm_start_used"] / run.n],
+            "drift_max_vs_oracle": worst, "drift_cells_per_step": run.drift_sample,
+            "train": run.report.get("train")}
 
 
 def main():
@@ -203,8 +349,14 @@ def main():
     step = ReactionStep(net, opt, device=local)
     pristine = host.to_device()
     dev = pristine.copy()
+    tune = None
     if args.autotune:
-        step.autotune(dev, dt)
+        # the launch search runs on its own draw of the workload
+        _, _, th, _ = make_workload(min(262144, n), device=f"cuda:{local}", rank=rank, seed=4049)
+        t0 = time.perf_counter()
+        step.autotune(th.to_device(), dt)
+        tune = {"cells": th.ncells, "s": time.perf_counter() - t0}
+        del th
     launch = step.launch()
 
     def restore():
@@ -218,7 +370,7 @@ def main():
             restore()
             step.react(dev, dt)
         torch.cuda.synchronize()
-        dev_ms, iters, alt, slots, drains = [], [], [], [], []
+        r = {"ms": [], "iters": [], "alt": [], "slots": [], "drain": [], "conv": []}
         with Clocks(clk_index) as clk:
             for _ in range(args.steps):
                 restore()
@@ -227,22 +379,26 @@ def main():
                     torch.distributed.barrier()
                 step.react(dev, dt)
                 st = step.stats()
-                dev_ms.append(st.kernel_ms)
-                iters.append(st.sum_iterations)
-                alt.append(st.alt_guess_used)
-                slots.append(st.lane_slots)
-                drains.append(st.drain_ms)
+                r["ms"].append(st.kernel_ms)
+                r["iters"].append(st.sum_iterations)
+                r["alt"].append(st.alt_guess_used)
+                r["slots"].append(st.lane_slots)
+                r["drain"].append(st.drain_ms)
+                r["conv"].append(st.ncells - st.nonconverged)
                 torch.cuda.synchronize()
-        eff = float(np.sum(iters)) / float(np.sum(slots)) if np.sum(slots) else None
-        timed.drain_ms = float(np.mean(drains))
-        return float(np.sum(dev_ms)), iters, alt, clk.summary(), eff
+        r["clocks"] = clk.summary()
+        r["total_ms"] = float(np.sum(r["ms"]))
+        r["eff"] = float(np.sum(r["iters"])) / float(np.sum(r["slots"])) if np.sum(r["slots"]) else None
+        r["drain_ms"] = float(np.mean(r["drain"]))
+        r["value"] = world * float(np.sum(r["conv"])) / (r["total_ms"] * 1e-3)
+        r["nonconverged"] = int(n - r["conv"][-1])
+        return r
 
     # plain Newton from the previous-step guess
-    plain_ms, plain_iters, _, plain_clocks, plain_eff = timed(local)
-    plain_drain = timed.drain_ms
-    plain_value = world * n / (plain_ms / args.steps * 1e-3)
+    plain = timed(local)
     g_plain = dev.to_host()
     warm = None
+    pred_sample = None
     if not args.plain_only:
         # learned warm start: trained on solves of a fresh seeded draw by the same kernel
         from pflotran_gb300 import surrogate, workloads
@@ -261,56 +417,63 @@ def main():
         err = (torch.log(pred) - torch.log(sol))[:, ok].abs()
         plain_guess = torch.from_numpy(host.pri_molal).to(pred.device).view(net.N, n)
         err0 = (torch.log(plain_guess) - torch.log(sol))[:, ok].abs()
+        if not args.no_cpu and rank == 0:
+            pidx = sample_indices(n, args.cpu_sample)
+            pred_sample = pred[:, torch.as_tensor(pidx, device=pred.device)].cpu().numpy().copy()
+        del pred
         step.surrogate_enable(True)
-        if args.autotune:
-            restore()
-            step.autotune(dev, dt)
         warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),
                     err0_rms=float(err0.pow(2).mean().sqrt()), err0_p50=float(err0.max(0).values.median()))
-    total_ms, iters, alt, clocks, eff = (timed(local) if warm is not None
-                                         else (plain_ms, plain_iters, [0], plain_clocks, plain_eff))
-    drain = timed.drain_ms if warm is not None else plain_drain
-    launch = step.launch()
+        del err, err0, sol, plain_guess
+    head = timed(local) if warm is not None else plain
     g = dev.to_host()
+
+    # RReact's damped path (exact_jacobian_after = 0), plain
+    refpath = None
+    g_ref = None
+    if args.reference_path and args.jacobian == "reference":
+        if warm is not None:
+            step.surrogate_enable(False)
+        step.set_options(_opts(opt, exact_jacobian_after=0))
+        rp = timed(local)
+        g_ref = dev.to_host()
+        refpath = {"value": rp["value"], "ms_per_step": rp["total_ms"] / args.steps,
+                   "mean_newton_iterations": float(np.mean(rp["iters"])) / n,
+                   "nonconverged": rp["nonconverged"], "queue_drain_ms": rp["drain_ms"],
+                   "lane_efficiency": rp["eff"], "max_iterations": int(g_ref.iterations.max())}
+        step.set_options(opt)
+        if warm is not None:
+            step.surrogate_enable(True)
     exact = None
     if args.exact_jacobian:
         # the same step with the exact Newton Jacobian (same equations and root)
         from pflotran_gb300 import abi
-        from pflotran_gb300.network import default_options
-        step.set_options(default_options(use_isothermal=opt.use_isothermal, jacobian=abi.JACOBIAN_EXACT))
+        step.set_options(_opts(opt, jacobian=abi.JACOBIAN_EXACT))
         exact = {}
         for mode in (("plain", "warm") if warm is not None else ("plain",)):
             if warm is not None:
                 step.surrogate_enable(mode == "warm")
-            if args.autotune:
-                restore()
-                step.autotune(dev, dt)
-            ms, its, _, _, e_eff = timed(local)
+            r = timed(local)
             ge = dev.to_host()
-            both = (ge.status == 0) & (g.status == 0)
-            rel = np.abs(ge.total_out - g.total_out).reshape(net.N, n) / np.maximum(
-                np.abs(g.total_out).reshape(net.N, n), 1e-300)
-            exact[mode] = {"value": world * n / (ms / args.steps * 1e-3), "ms_per_step": ms / args.steps,
-                           "mean_newton_iterations": float(np.mean(its)) / n,
+            exact[mode] = {"value": r["value"], "ms_per_step": r["total_ms"] / args.steps,
+                           "mean_newton_iterations": float(np.mean(r["iters"])) / n,
                            "max_newton_iterations": int(ge.iterations.max()),
-                           "lane_efficiency": e_eff, "queue_drain_ms": timed.drain_ms,
-                           "nonconverged": int((ge.status != 0).sum()),
-                           "total_rel_diff_vs_reference_jacobian_max": float(rel[:, both].max())}
+                           "lane_efficiency": r["eff"], "queue_drain_ms": r["drain_ms"],
+                           "nonconverged": r["nonconverged"]}
         if warm is not None:
             exact["speedup_warm_vs_plain"] = exact["warm"]["value"] / exact["plain"]["value"]
-            exact["speedup_vs_reference_jacobian_warm"] = exact["warm"]["value"] / (world * n / (total_ms / args.steps * 1e-3))
         step.set_options(opt)
-        step.set_launch(launch.block_threads, launch.blocks_per_sm, launch.refill_min_idle, launch.variant)
         if warm is not None:
             step.surrogate_enable(True)
+    total_ms = head["total_ms"]
     if world > 1:
         t = torch.tensor([total_ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step * 1e-3)
-    conv = int((g.status == 0).sum())
+    conv_per_step = float(np.mean(head["conv"]))
+    value = world * conv_per_step / (ms_per_step * 1e-3)
 
     # end-to-end through the public API with pinned host buffers
     pinned = CellBatch(n)
@@ -331,7 +494,7 @@ def main():
               if getattr(pinned, f) is not None)
     state_fields = ("pri_molal", "ionic_strength", "mnrl_volfrac", "total_sorb_eq",
                     "eqionx_ref_cation_sorbed_conc", "srfcplxrxn_free_site_conc")
-    e2e_s = []
+    e2e_s, e2e_conv = [], []
     for s in range(args.warmup + args.steps):
         for f in state_fields:
             a = getattr(pinned, f)
@@ -339,14 +502,15 @@ def main():
                 a[:] = getattr(host, f)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        step.react(pinned, dt)
+        bad = step.react(pinned, dt)
         el = time.perf_counter() - t0
         if s >= args.warmup:
             e2e_s.append(el)
-    e2e_value = world * n / (sum(e2e_s) / len(e2e_s))
+            e2e_conv.append(n - bad)
+    e2e_value = world * float(np.mean(e2e_conv)) / (sum(e2e_s) / len(e2e_s))
 
     # roofline: FP64-issue bound; algorithmic flops per launch / device time
-    mean_iters = float(np.mean(iters)) / n
+    mean_iters = float(np.mean(head["iters"])) / n
     flops = work.step_flops(net, g.iterations, isothermal=bool(opt.use_isothermal))
     achieved_tflops = flops / (ms_per_step * 1e-3) / 1e12
     probe = fp64_peak(local)
@@ -361,11 +525,12 @@ def main():
     wline = None
     if warm is not None:
         r = warm["report"]
-        wline = {"plain_value": plain_value, "plain_ms_per_step": plain_ms / args.steps,
-                 "plain_mean_newton_iterations": float(np.mean(plain_iters)) / n,
-                 "plain_lane_efficiency": plain_eff, "plain_queue_drain_ms": plain_drain,
-                 "speedup_vs_plain": value / plain_value,
-                 "alt_guess_used_frac": float(np.mean(alt)) / n,
+        wline = {"plain_value": plain["value"], "plain_ms_per_step": plain["total_ms"] / args.steps,
+                 "plain_mean_newton_iterations": float(np.mean(plain["iters"])) / n,
+                 "plain_nonconverged": plain["nonconverged"],
+                 "plain_lane_efficiency": plain["eff"], "plain_queue_drain_ms": plain["drain_ms"],
+                 "speedup_vs_plain": value / plain["value"],
+                 "alt_guess_used_frac": float(np.mean(head["alt"])) / n,
                  "surrogate": {"arch": "16-256-256-256-12 GELU MLP, BF16 weights/activations, FP32 accumulate "
                                        "(mma.sync m16n8k16)",
                                "train_samples": int(r.samples), "epochs": args.epochs, "steps": int(r.steps),
@@ -380,13 +545,16 @@ def main():
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"synthetic 12-species network (40 complexes, 6 minerals, 4 ion-exchange, "
                                f"2 surface-complexation), {n} cells per GPU, dt 1 day, plain Newton from the "
-                               f"previous-step guess, 1e-12 rel. residual",
+                               f"previous-step guess, 1e-12 rel. residual, exact_jacobian_after "
+                               f"{opt.exact_jacobian_after}; converged cells counted",
                    "ncells": n, "l2": "inputs ~1.3 GB >> L2; state restored from a pristine copy between steps",
                    "launch": {"block_threads": launch.block_threads, "blocks_per_sm": launch.blocks_per_sm,
-                              "refill_min_idle": launch.refill_min_idle},
+                              "refill_min_idle": launch.refill_min_idle, "variant": launch.variant,
+                              "source": "pfchem_autotune" if tune else "library default", "autotune": tune},
                    "parallelism": "replicas" if world > 1 else "single"},
-        "mean_newton_iterations": mean_iters, "converged_cells": conv,
-        "lane_efficiency": eff, "queue_drain_ms": drain,
+        "mean_newton_iterations": mean_iters, "converged_cells": int((g.status == 0).sum()),
+        "nonconverged": head["nonconverged"],
+        "lane_efficiency": head["eff"], "queue_drain_ms": head["drain_ms"],
         "iteration_histogram": np.bincount(g.iterations).tolist(),
         # per step: prologue + persistent solve; the warm start adds the weight
         # packing (one launch per layer) and the fused MLP inference
@@ -401,11 +569,13 @@ def main():
                      "flops_per_step": flops,
                      "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
                              "bytes_per_step": bytes_step, "peak_source": "MEASURED_PEAKS.json hbm_gbs"}},
-        "clocks": clocks,
+        "clocks": head["clocks"],
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
     }
     if exact is not None:
         line["exact_jacobian"] = exact
+    if refpath is not None:
+        line["reference_path"] = refpath
     if args.jacobian == "exact":
         line["config"]["workload"] += ", exact Newton Jacobian (PFCHEM_JACOBIAN_EXACT)"
     if wline is not None:
@@ -414,8 +584,40 @@ def main():
             "plain Newton from the previous-step guess", "learned BF16 warm start with per-cell fallback, "
                                                          "FP64 Newton finishing")
     if rank == 0 and not args.no_cpu:
-        cb, _ = cpu_baseline(net, opt, host, dt, args.cpu_sample)
+        from oracle import parity
+        cb, idx, sub, ref = cpu_baseline(net, opt, host, dt, args.cpu_sample)
         line["cpu_baseline"] = cb
+        truth = parity.truth_solve(net, opt, dt, sub, ref)
+        par = {"sample": f"{len(idx)} cells drawn at random (seed {SAMPLE_SEED})",
+               "root": f"oracle in long double, exact undamped Newton to a 1e-16 relative residual from the "
+                       f"oracle's solution; {int((truth.status == 0).sum())} cells solved",
+               "plain": parity_block(net, opt, dt, sub, ref, g_plain.subset(idx, net), truth)}
+        if warm is not None and pred_sample is not None:
+            ref_w = parity.solve(net, opt, dt, sub, 0, alt_guess=pred_sample.ravel())
+            par["warm"] = parity_block(net, opt, dt, sub, ref_w, g.subset(idx, net), truth)
+            both = (ref.status == 0) & (g.subset(idx, net).status == 0)
+            par["warm_vs_plain_oracle"] = parity.error_statement(net, g.subset(idx, net), ref, both)
+        line["parity"] = par
+        if g_ref is not None:
+            # RReact's damped path: the cells the 200-iteration cap stops,
+            # against RReact without a cap
+            capped = np.flatnonzero(g_ref.status != 0)
+            if len(capped):
+                cs = capped[sample_indices(len(capped), 2000, SAMPLE_SEED + 2)]
+                hsub = host.subset(cs, net)
+                free = parity.solve(net, _opts(opt, exact_jacobian_after=0, max_iterations=1_000_000), dt, hsub)
+                ok = free.status == 0
+                e = parity.cell_errors(net, g_ref.subset(cs, net), free)["total"]
+                line["reference_path"]["capped_cells"] = {
+                    "sampled": len(cs), "converge_without_cap": int(ok.sum()),
+                    "uncapped_iterations_p50_p99_max": [float(np.percentile(free.iterations[ok], q))
+                                                        for q in (50, 99, 100)] if ok.any() else None,
+                    "capped_answer_vs_uncapped_total_median_max": [float(np.median(e[ok])), float(e[ok].max())]
+                    if ok.any() else None}
+    if rank == 0 and args.calcite_grid:
+        line["calcite_grid"] = calcite_grid(args, local)
+    if rank == 0 and args.timestepped:
+        line["timestepped"] = timestepped(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

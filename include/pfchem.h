@@ -406,7 +406,13 @@ typedef struct pfchem_launch {
 int pfchem_get_launch(const pfchem_ctx *ctx, pfchem_launch *launch);
 int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
 /* Times candidate mappings on `cells` (device pointers; the state arrays are
- * restored after every trial) and keeps the fastest. */
+ * restored after every trial) and keeps the fastest: 32 or 64 threads per
+ * block, the augmented or the compact shared-memory layout of the
+ * network-specialized kernel (the candidates compiled concurrently), as many
+ * resident blocks per SM as fit or one fewer, and a refill at 1, 2, 4 or 8
+ * idle lanes; each candidate runs twice and its faster run counts.  Every
+ * candidate computes each cell with the same operations, so the answers do
+ * not depend on the choice. */
 int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
 
 /* ---------------------------------------------------------------------------
@@ -484,10 +490,16 @@ int pfchem_check_specialized(const pfchem_network *net, const pfchem_options *op
  * its only global scratch is a static device array of
  * PFCHEM_NOALLOC_SCRATCH_BYTES bytes, held by every GPU that loads the
  * library until exit, and launches needing more are rejected (-1, message in
- * err).  The first call on a device looks up that array's address; make it
- * before any stream capture.  All calls share the array: calls that overlap
- * on the GPU race, so serialise them.  `stats` may be NULL (kernel_ms is not
- * measured).  Returns as pfchem_react_batch; error text goes to err[errlen]. */
+ * err).  The first call on a device looks up that array's address.  Every
+ * call copies its statistics to host memory and synchronises `stream`
+ * before it returns, so it blocks and can never be captured into a CUDA
+ * graph (graph users: pfchem_react_batch_async).  All calls share the array:
+ * calls that overlap on one GPU race, so serialise them.  It runs the
+ * table-driven solve kernel, about 2.6x slower than pfchem_react_batch's
+ * network-specialized kernel on the 12-species network (918 vs 354 ms per
+ * step at 2,097,152 cells).  `stats` may be NULL; it is zeroed first and
+ * kernel_ms, lane_slots and drain_ms stay 0.  Returns as pfchem_react_batch;
+ * error text goes to err[errlen]. */
 int pfchem_react_batch_noalloc(const pfchem_network *net, const pfchem_options *opt, double dt,
                                pfchem_cells *cells, void *stream, pfchem_stats *stats, char *err,
                                size_t errlen);

@@ -14,6 +14,7 @@
 #include <string>
 #include <vector>
 #include <random>
+#include <utility>
 #include <nvrtc.h>
 
 #include "../../include/pfchem.h"
@@ -30,6 +31,7 @@ cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *r
                                    double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
 int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **pro_out, std::string *err);
+int gen_kernels_prepare(const DevNet &n, const std::vector<std::pair<int, bool>> &cands, std::string *err);
 int gen_prep_fields(const DevNet &n);
 int gen_blocks_per_sm(void *fn, const DevNet &n, int block, bool compact);
 size_t gen_shared_bytes(const DevNet &n, int block, bool compact);
@@ -871,30 +873,51 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
       return fail(c, -2, "autotune state backup: %s", cudaGetErrorString(ae));
     }
   }
-  const int blocks[] = {32, 64, 128};
-  const int refills[] = {1, 4, 8, 16, 32};
+  // candidates: block of 32 or 64 threads, augmented or compact shared-memory
+  // layout (compiled concurrently), as many resident blocks per SM as fit or
+  // one fewer, refill at 1, 2, 4 or 8 idle lanes; each timed twice (the
+  // faster run counts), the state restored after every run
+  const int blocks[] = {32, 64};
+  const int refills[] = {1, 2, 4, 8};
+  std::vector<std::pair<int, bool>> cands;
+  for (int variant : {PFCHEM_KERNEL_SPECIALIZED, PFCHEM_KERNEL_SPECIALIZED_COMPACT})
+    for (int b : blocks) {
+      const bool cmp = variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT;
+      if (gen_shared_bytes(n, b, cmp) <= 227 * 1024) cands.push_back({b, cmp});
+    }
+  {
+    std::string err;
+    if (gen_kernels_prepare(n, cands, &err)) {
+      for (auto &x : arrs) cudaFree(x.save);
+      return fail(c, -2, "specialized kernel: %s", err.c_str());
+    }
+  }
   double best = 1e30;
   pfchem_launch best_l = c->launch;
   int rc = 0;
-  for (int variant : {PFCHEM_KERNEL_SPECIALIZED, PFCHEM_KERNEL_SPECIALIZED_COMPACT}) {
-    const bool cmp = variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT;
-    for (int b : blocks) {
-      if (gen_shared_bytes(n, b, cmp) > 227 * 1024) continue;
-      int nb = ensure_gen(c, b, cmp);
-      if (nb < 1) continue;
+  for (const auto &cand : cands) {
+    const int b = cand.first;
+    const bool cmp = cand.second;
+    const int variant = cmp ? PFCHEM_KERNEL_SPECIALIZED_COMPACT : PFCHEM_KERNEL_SPECIALIZED;
+    const int nb = ensure_gen(c, b, cmp);
+    if (nb < 1) continue;
+    for (int bps = nb; bps >= std::max(1, nb - 1) && rc >= 0; --bps) {
       for (int r : refills) {
-        pfchem_launch l{b, nb, r, variant};
+        pfchem_launch l{b, bps, r, variant};
         c->launch = l;
-        rc = pfchem_react_batch(c, dt, cl);
+        double ms = 1e30;
+        for (int rep = 0; rep < 2; ++rep) {
+          rc = pfchem_react_batch(c, dt, cl);
+          if (rc < 0) break;
+          ms = std::min(ms, c->stats.kernel_ms);
+          for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+        }
         if (rc < 0) break;
-        const double ms = c->stats.kernel_ms;
         if (ms < best) {
           best = ms;
           best_l = l;
         }
-        for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
       }
-      if (rc < 0) break;
     }
     if (rc < 0) break;
   }

@@ -34,7 +34,8 @@
 #include <mutex>
 #include <sstream>
 #include <string>
-#include <vector>
+#include <thread>
+#include <utility>
 #include <vector>
 
 #include "pfchem_device.cuh"
@@ -1124,21 +1125,11 @@ size_t gen_shared_bytes(const DevNet &n, int block, bool compact) {
   return ((size_t)n.N * (n.N + 1) + n.N) * block * sizeof(double);
 }
 
-// Compiles (or fetches from the per-process cache) the specialized kernel for
-// `n` and `block` threads per block on the current device.
-int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **pro_out, std::string *err) {
-  int dev = 0;
-  cudaGetDevice(&dev);
-  cudaFree(0);  // make the device's primary context current for the driver API
-  const std::string src = generate_source(n, block, compact);
-  const std::string key = std::to_string(dev) + ":" + std::to_string(block) + ":" + src;
-  std::lock_guard<std::mutex> lock(g_cache_mutex);
-  auto it = g_cache.find(key);
-  if (it != g_cache.end()) {
-    *fn_out = (void *)it->second.fn;
-    *pro_out = (void *)it->second.pro;
-    return 0;
-  }
+namespace {
+
+// NVRTC compile of one generated source to a cubin (no shared state: runs
+// concurrently for several candidates).
+int compile_cubin(const std::string &src, std::vector<char> *cubin, std::string *err) {
   nvrtcProgram prog;
   if (nvrtcCreateProgram(&prog, src.c_str(), "pfchem_gen.cu", 0, nullptr, nullptr) != NVRTC_SUCCESS) {
     *err = "nvrtcCreateProgram failed";
@@ -1158,9 +1149,15 @@ int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **p
   }
   size_t cs = 0;
   nvrtcGetCUBINSize(prog, &cs);
-  std::vector<char> cubin(cs);
-  nvrtcGetCUBIN(prog, cubin.data());
+  cubin->resize(cs);
+  nvrtcGetCUBIN(prog, cubin->data());
   nvrtcDestroyProgram(&prog);
+  return 0;
+}
+
+// Loads a cubin into the current context and caches it under `key`
+// (g_cache_mutex held by the caller).
+int load_cubin(const std::string &key, const std::vector<char> &cubin, Loaded *out, std::string *err) {
   const Driver &D = driver();
   if (!D.ok) {
     *err = "CUDA driver entry points unavailable";
@@ -1182,9 +1179,84 @@ int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **p
   }
   D.funcSetAttribute(L.fn, CU_FUNC_ATTRIBUTE_MAX_DYNAMIC_SHARED_SIZE_BYTES, 227 * 1024);
   g_cache[key] = L;
+  *out = L;
+  return 0;
+}
+
+std::string cache_key(int dev, int block, const std::string &src) {
+  return std::to_string(dev) + ":" + std::to_string(block) + ":" + src;
+}
+
+}  // namespace
+
+// Compiles (or fetches from the per-process cache) the specialized kernel for
+// `n` and `block` threads per block on the current device.
+int gen_kernel(const DevNet &n, int block, bool compact, void **fn_out, void **pro_out, std::string *err) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaFree(0);  // make the device's primary context current for the driver API
+  const std::string src = generate_source(n, block, compact);
+  const std::string key = cache_key(dev, block, src);
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mutex);
+    auto it = g_cache.find(key);
+    if (it != g_cache.end()) {
+      *fn_out = (void *)it->second.fn;
+      *pro_out = (void *)it->second.pro;
+      return 0;
+    }
+  }
+  std::vector<char> cubin;
+  if (compile_cubin(src, &cubin, err)) return -2;
+  std::lock_guard<std::mutex> lock(g_cache_mutex);
+  auto it = g_cache.find(key);  // compiled meanwhile by another thread
+  Loaded L;
+  if (it != g_cache.end()) L = it->second;
+  else if (load_cubin(key, cubin, &L, err)) return -2;
   *fn_out = (void *)L.fn;
   *pro_out = (void *)L.pro;
   return 0;
+}
+
+// Compiles the specialized kernels of several (block, compact) candidates
+// concurrently (one NVRTC program per thread) and caches them; the first
+// error, if any, goes to `err`.
+int gen_kernels_prepare(const DevNet &n, const std::vector<std::pair<int, bool>> &cands, std::string *err) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaFree(0);
+  std::vector<std::string> keys(cands.size());
+  std::vector<std::vector<char>> bins(cands.size());
+  std::vector<std::string> errs(cands.size());
+  std::vector<int> rcs(cands.size(), 0);
+  std::vector<std::thread> pool;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    const std::string src = generate_source(n, cands[i].first, cands[i].second);
+    keys[i] = cache_key(dev, cands[i].first, src);
+    {
+      std::lock_guard<std::mutex> lock(g_cache_mutex);
+      if (g_cache.count(keys[i])) continue;
+    }
+    pool.emplace_back([&, i, src]() { rcs[i] = compile_cubin(src, &bins[i], &errs[i]); });
+  }
+  for (auto &t : pool) t.join();
+  std::lock_guard<std::mutex> lock(g_cache_mutex);
+  int rc = 0;
+  for (size_t i = 0; i < cands.size(); ++i) {
+    if (rcs[i]) {
+      if (!rc) *err = errs[i];
+      rc = -2;
+      continue;
+    }
+    if (bins[i].empty() || g_cache.count(keys[i])) continue;
+    Loaded L;
+    std::string e;
+    if (load_cubin(keys[i], bins[i], &L, &e)) {
+      if (!rc) *err = e;
+      rc = -2;
+    }
+  }
+  return rc;
 }
 
 int gen_prep_fields(const DevNet &n) {

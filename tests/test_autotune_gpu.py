@@ -1,0 +1,36 @@
+"""The launch autotuner on a 32,768-cell draw of the 12-species workload:
+the launch it keeps is no slower than the library's default launch, and the
+answers do not depend on the launch."""
+import numpy as np
+import pytest
+
+from pflotran_gb300 import workloads
+from pflotran_gb300.lib import ReactionStep
+
+pytestmark = pytest.mark.gpu
+
+
+def _timed(step, cells, dt, reps=3):
+    best, out = 1e30, None
+    for _ in range(reps):
+        d = cells.to_device()
+        step.react(d, dt)
+        best = min(best, step.stats().kernel_ms)
+        out = d.to_host()
+    return best, out
+
+
+def test_autotuned_launch_is_no_slower_and_bit_identical():
+    net, opt, cells, dt = workloads.synthetic_cells(32768, seed=77)
+    step = ReactionStep(net, opt)
+    default = step.launch()
+    t_default, a = _timed(step, cells, dt)
+    _, _, trial, _ = workloads.synthetic_cells(32768, seed=78, net=net)
+    tuned = step.autotune(trial.to_device(), dt)
+    t_tuned, b = _timed(step, cells, dt)
+    print(f"default {default.block_threads}/{default.blocks_per_sm}/{default.refill_min_idle}/{default.variant} "
+          f"{t_default:.3f} ms, tuned {tuned.block_threads}/{tuned.blocks_per_sm}/{tuned.refill_min_idle}/"
+          f"{tuned.variant} {t_tuned:.3f} ms")
+    assert t_tuned <= 1.10 * t_default, (t_tuned, t_default)
+    for f in ("pri_molal", "total_out", "mnrl_rate", "mnrl_volfrac", "total_sorb_eq", "iterations", "status"):
+        np.testing.assert_array_equal(getattr(a, f), getattr(b, f), err_msg=f)

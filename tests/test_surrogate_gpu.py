@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from oracle import mlp_oracle as mo
+from oracle import parity
 from pflotran_gb300 import workloads
 from pflotran_gb300.lib import ReactionStep
 from pflotran_gb300.surrogate import fit, generate
@@ -46,6 +47,7 @@ def test_gradients_match_fp64_oracle():
             if np.linalg.norm(b) == 0:
                 continue
             rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+            print(f"layer {l} {'weights' if size == k * n else 'bias'}: relative L2 error {rel:.3e}")
             assert rel < 2e-2, (l, size, rel)
 
 
@@ -85,33 +87,30 @@ def test_trained_warm_start_reduces_iterations_with_identical_results(oracle):
     step.surrogate_enable(True)
     step.react(warm, dt)
     st_warm = step.stats()
-    gp, gw = plain.to_host(), warm.to_host()
+    gw = warm.to_host()
     mean_plain = st_plain.sum_iterations / cells.ncells
     mean_warm = st_warm.sum_iterations / cells.ncells
     assert st_warm.alt_guess_used > 0.5 * cells.ncells
     assert mean_warm < 0.9 * mean_plain, (mean_plain, mean_warm)
-    # both solves are roots of the same equations to a 1e-12 relative
-    # residual; from different starting points they agree to about
-    # tolerance x conditioning
-    ok = (gp.status == 0) & (gw.status == 0)
-    rel = np.abs(gw.pri_molal - gp.pri_molal) / gp.pri_molal
-    assert rel.reshape(net.N, -1)[:, ok].max() < 1e-8
-    # the warm-started path against the oracle given the same two guesses:
-    # the oracle applies the same choice (residual norm at both) and Newton
+    # the warm-started path against the oracle given the same two guesses
+    # (the oracle applies the same choice, residual norm at both, and
+    # Newton), on 4096 cells; bar per cell at 1e-10: within 1e-10 of that
+    # oracle solution, or no farther than it from the root of the cell's
+    # equations (long double, 1e-16 relative residual).  A cell whose last
+    # residual lands next to the 1e-12 threshold may stop one iteration apart
+    # on the two machines; the second branch covers it.
     sub_idx = np.arange(4096)
-    ref = cells.subset(sub_idx, net)
-    ref.alt_guess = np.ascontiguousarray(pred.reshape(net.N, -1)[:, sub_idx]).ravel()
-    ref.sec_molal = np.zeros(net.Nc * len(sub_idx))
-    oracle.react(net.as_struct(), opt, dt, ref, 0, 8)
+    sub = cells.subset(sub_idx, net)
+    ref = parity.solve(net, opt, dt, sub, alt_guess=np.ascontiguousarray(pred.reshape(net.N, -1)[:, sub_idx]).ravel())
     g_sub = gw.subset(sub_idx, net)
     ok = (ref.status == 0) & (g_sub.status == 0)
-    assert ok.mean() > 0.95
-    same = ok & (ref.iterations == g_sub.iterations)
-    assert same.sum() > 0.98 * ok.sum()
+    assert ok.all()
+    same = ref.iterations == g_sub.iterations
+    assert same.mean() > 0.98
     errs = compare(net, g_sub, ref, mask=same)
     assert all(v <= 1e-10 for v in errs.values()), errs
-    # a cell whose last residual lands next to the 1e-12 threshold may stop one
-    # iteration apart on the two machines: the answers then differ by that
-    # last step, inside the convergence tolerance x conditioning
-    errs = compare(net, g_sub, ref, mask=ok)
-    assert all(v <= 1e-9 for v in errs.values()), errs
+    plain_ref = parity.solve(net, opt, dt, sub)
+    truth = parity.truth_solve(net, opt, dt, sub, plain_ref)
+    assert (truth.status == 0).all()
+    for q, (bar, *_rest) in parity.per_cell_bar(net, g_sub, ref, truth).items():
+        assert bar.all(), (q, int((~bar).sum()))
