@@ -136,6 +136,20 @@ int activity_coefficients(const Net &w, const pfchem_options &o, Cell<R> &c, boo
   }
   const R A = n.debyeA, B = n.debyeB, Bdot = n.debyeBdot;
   if (o.act_coef_update_algorithm == PFCHEM_ACT_COEF_ALGORITHM_NEWTON) {
+    if (use_I_start) {
+      // The step's entry state at the library's boundary, which carries the
+      // ionic strength rather than the activity coefficients: the primaries'
+      // coefficients at that ionic strength and no complexes yet (the first
+      // pass of the loop below then keeps I = I_start exactly).
+      const R sI = std::sqrt(I_start);
+      for (int j = 0; j < N; ++j) {
+        const R z = n.primary_spec_Z[j];
+        c.pri_act_coef[j] = std::fabs(z) > 0 ? rexp((-z * z * sI * A / (R(1) + R(n.primary_spec_a0[j]) * B * sI) +
+                                                      Bdot * I_start) * R(kLOG_TO_LN))
+                                             : R(1);
+      }
+      for (int i = 0; i < Nc; ++i) c.sec_molal[i] = 0;
+    }
     R ln_conc[P], ln_act[P];
     for (int j = 0; j < N; ++j) {
       ln_conc[j] = rlog(c.pri_molal[j]);
@@ -618,7 +632,9 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
     }
     if (!compute_derivative) continue;
     R dIm_dQK;
-    if (w.exact_jac && lnQK > R(6.90776)) continue;  // QK capped: the rate does not depend on m
+    // exact: where QK is capped the rate does not depend on QK (the
+    // prefactor terms below still apply)
+    const bool qk_terms = !(w.exact_jac && lnQK > R(6.90776));
     if (n.kinmnrl_affinity_power)
       dIm_dQK = -Im * R(n.kinmnrl_affinity_power[m]) / (w.exact_jac ? affinity_factor : std::fabs(affinity_factor));
     else
@@ -631,7 +647,8 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
     } else if (n.kinmnrl_min_scale_factor) {
       dIm_dQK = dIm_dQK * (R(1) / R(n.kinmnrl_min_scale_factor[m])) / QK * (R(1) - affinity_factor);
     }
-    if (n.kinmnrl_rate_limiter[m] <= 0) {
+    if (!qk_terms) {
+    } else if (n.kinmnrl_rate_limiter[m] <= 0) {
       for (int j = 1; j <= ncomp; ++j) {
         int jc = w.mid(m, j);
         R dQK_dCj = R(w.mnu(m, j)) * QK * rexp(-ln_conc[jc]);
@@ -693,7 +710,12 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
           } else {
             // reaction_mineral.F90:958-991: derivative through a secondary
             // species.  The reference reuses `ncomp` and `icomp` here, so the
-            // species loops below run over the complex's own species.
+            // species loops below run over the complex's own species: the
+            // rows are the complex's species with its stoichiometry.  The
+            // exact Jacobian puts the same column derivative into the
+            // mineral's rows.  (A primary prefactor species listed after a
+            // secondary one in the same mineral would, in the reference, loop
+            // over the complex's species count; here it uses the mineral's.)
             int icplx = -icomp - 1;
             R lq = -c.eqcplx_logK[icplx] * R(kLOG_TO_LN);
             if (n.eqcplxh2oid && n.eqcplxh2oid[icplx] > 0) lq = lq + R(n.eqcplxh2ostoich[icplx]) * c.ln_act_h2o;
@@ -702,9 +724,16 @@ void kinetic_mineral(const Net &w, Cell<R> &c, R *Res, R (*Jac)[P], bool compute
             for (int j = 1; j <= ncx; ++j) {
               int jc = w.cid(icplx, j);
               R t = R(w.cnu(icplx, j)) * rexp(lq - ln_conc[jc]) / c.sec_act_coef[icplx];
-              for (int i = 1; i <= ncx; ++i) {
-                int ic = w.cid(icplx, i);
-                Jac[ic][jc] = Jac[ic][jc] + R(w.cnu(icplx, i)) * t * dIm_dspec;
+              if (w.exact_jac) {
+                for (int i = 1; i <= ncomp; ++i) {
+                  int ic = w.mid(m, i);
+                  Jac[ic][jc] = Jac[ic][jc] + R(w.mnu(m, i)) * t * dIm_dspec;
+                }
+              } else {
+                for (int i = 1; i <= ncx; ++i) {
+                  int ic = w.cid(icplx, i);
+                  Jac[ic][jc] = Jac[ic][jc] + R(w.cnu(icplx, i)) * t * dIm_dspec;
+                }
               }
             }
           }

@@ -131,12 +131,12 @@ int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o
   if (w->neqionxrxn < 0 || w->neqionxrxn > PFCHEM_MAX_IONX) return fail(c, -1, "neqionxrxn %d > %d", w->neqionxrxn, PFCHEM_MAX_IONX);
   if (w->nsrfcplxrxn < 0 || w->nsrfcplxrxn > PFCHEM_MAX_SRFRXN) return fail(c, -1, "nsrfcplxrxn %d > %d", w->nsrfcplxrxn, PFCHEM_MAX_SRFRXN);
   if (w->nsrfcplx < 0 || w->nsrfcplx > PFCHEM_MAX_SRFCPLX) return fail(c, -1, "nsrfcplx %d > %d", w->nsrfcplx, PFCHEM_MAX_SRFCPLX);
-  if (w->max_num_prefactors > 0 && w->kinmnrl_num_prefactors) {
-    for (int m = 0; m < w->nkinmnrl; ++m)
-      if (w->kinmnrl_num_prefactors[m] > 0) return fail(c, -1, "mineral %d: rate prefactors are not supported by the device kernels", m + 1);
-  }
-  if (o->act_coef_update_algorithm == PFCHEM_ACT_COEF_ALGORITHM_NEWTON && o->act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF)
-    return fail(c, -1, "ACT_COEF_ALGORITHM_NEWTON is not supported by the device kernels (use LAG)");
+  if (o->act_coef_update_algorithm != PFCHEM_ACT_COEF_ALGORITHM_LAG &&
+      o->act_coef_update_algorithm != PFCHEM_ACT_COEF_ALGORITHM_NEWTON)
+    return fail(c, -1, "unknown act_coef_update_algorithm %d", o->act_coef_update_algorithm);
+  if (o->act_coef_update_algorithm == PFCHEM_ACT_COEF_ALGORITHM_NEWTON && o->use_activity_h2o &&
+      o->act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF)
+    return fail(c, -1, "use_activity_h2o with ACT_COEF_ALGORITHM_NEWTON is not supported");
   if (o->use_activity_h2o && o->act_coef_update_frequency == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER)
     return fail(c, -1, "use_activity_h2o with NEWTON_ITER activity updates is not supported");
   if (o->max_iterations < 1) return fail(c, -1, "max_iterations must be >= 1");
@@ -148,6 +148,8 @@ int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o
   n.Nsc = w->nsrfcplx;
   n.use_log = o->use_log_formulation != 0;
   n.act_freq = o->act_coef_update_frequency;
+  n.act_newton = o->act_coef_update_algorithm == PFCHEM_ACT_COEF_ALGORITHM_NEWTON &&
+                 o->act_coef_update_frequency != PFCHEM_ACT_COEF_FREQUENCY_OFF;
   n.use_h2o = o->use_activity_h2o != 0;
   n.isothermal = o->use_isothermal != 0;
   n.resid_kind = o->residual_tol_kind;
@@ -218,6 +220,42 @@ int build_devnet(pfchem_ctx *c, const pfchem_network *w, const pfchem_options *o
     n.mtemkin[m] = n.has_temkin ? w->kinmnrl_Temkin_const[m] : 1.0;
     n.mscale[m] = n.has_minscale ? w->kinmnrl_min_scale_factor[m] : 1.0;
     n.mpow[m] = n.has_affpow ? w->kinmnrl_affinity_power[m] : 1.0;
+    // rate prefactors: tables (0:maxsp, maxpref, nkinmnrl) and (maxsp, maxpref, nkinmnrl)
+    const int np = (w->max_num_prefactors > 0 && w->kinmnrl_num_prefactors) ? w->kinmnrl_num_prefactors[m] : 0;
+    if (np < 0 || np > w->max_num_prefactors || np > PFCHEM_MAX_PREF)
+      return fail(c, -1, "mineral %d: %d rate prefactors outside [0, min(max_num_prefactors, %d)]", m + 1, np,
+                  PFCHEM_MAX_PREF);
+    n.mpn[m] = (int8_t)np;
+    if (np > 0) {
+      const int maxp = w->max_num_prefactors, maxs = w->max_num_prefactor_species;
+      if (!w->kinmnrl_pref_rate || !w->kinmnrl_pref_activation_energy || !w->kinmnrl_prefactor_id ||
+          !w->kinmnrl_pref_alpha || !w->kinmnrl_pref_beta || !w->kinmnrl_pref_atten_coef)
+        return fail(c, -1, "mineral %d: rate prefactor tables missing", m + 1);
+      n.has_pref = 1;
+      for (int p = 0; p < np; ++p) {
+        const int base = (maxs + 1) * (p + maxp * m);
+        const int ns = w->kinmnrl_prefactor_id[base];
+        if (ns < 0 || ns > maxs || ns > PFCHEM_MAX_PREF_SPEC)
+          return fail(c, -1, "mineral %d prefactor %d: %d species outside [0, min(max_num_prefactor_species, %d)]",
+                      m + 1, p + 1, ns, PFCHEM_MAX_PREF_SPEC);
+        n.mps[m][p] = (int8_t)ns;
+        n.mpk[m][p] = w->kinmnrl_pref_rate[p + maxp * m];
+        n.mpEa[m][p] = w->kinmnrl_pref_activation_energy[p + maxp * m];
+        for (int q = 0; q < ns; ++q) {
+          const int id = w->kinmnrl_prefactor_id[base + 1 + q];
+          if (id == 0 || id > n.N || -id > n.Nc)
+            return fail(c, -1, "mineral %d prefactor %d: species id %d outside [1,%d] or [-%d,-1]", m + 1, p + 1, id,
+                        n.N, n.Nc);
+          n.mpid[m][p][q] = (int8_t)(id > 0 ? id - 1 : id);
+          const int qq = q + maxs * (p + maxp * m);
+          n.mpa[m][p][q] = w->kinmnrl_pref_alpha[qq];
+          n.mpb[m][p][q] = w->kinmnrl_pref_beta[qq];
+          n.mpatt[m][p][q] = w->kinmnrl_pref_atten_coef[qq];
+          if (!(n.mpatt[m][p][q] >= 0.0))
+            return fail(c, -1, "mineral %d prefactor %d: negative attenuation coefficient", m + 1, p + 1);
+        }
+      }
+    }
   }
   if ((e = check_ids("ion exchange", w->eqionx_rxn_cationid, w->eqionx_ld, n.Nix, n.N))) return e;
   for (int r = 0; r < n.Nix; ++r) {
@@ -295,6 +333,14 @@ void default_launch(pfchem_ctx *c) {
 // Compiles (or reuses) the network-specialized kernel for `block` threads per
 // block and returns its resident blocks per SM (0 on failure, message in err).
 bool is_specialized(int v) { return v == PFCHEM_KERNEL_SPECIALIZED || v == PFCHEM_KERNEL_SPECIALIZED_COMPACT; }
+
+// The network-specialized kernel covers every option but the NEWTON activity
+// algorithm updated at every Newton iteration, which needs each complex's
+// concentration from the previous iteration (the table-driven kernel keeps
+// them).
+bool specialized_supports(const DevNet &n) {
+  return !(n.act_newton && n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER);
+}
 
 int ensure_gen(pfchem_ctx *c, int block, bool compact) {
   if (c->gen_fn && c->gen_block == block && c->gen_compact == compact)
@@ -623,9 +669,13 @@ int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_op
     c->graph = nullptr;
   }
   if (!c->launch_forced) {
-    // the network-specialized kernel is the default; a compile failure is an error
+    // the network-specialized kernel is the default (a compile failure is an
+    // error); the table-driven kernel where the specialized one does not apply
     default_launch(c);
-    if (default_specialized_launch(c) != 0) return -2;
+    if (specialized_supports(n) && default_specialized_launch(c) != 0) return -2;
+  } else if (is_specialized(c->launch.variant) && !specialized_supports(n)) {
+    return fail(c, -1, "the network-specialized kernel does not support the NEWTON activity algorithm at every "
+                       "Newton iteration; set a PFCHEM_KERNEL_GENERIC launch");
   } else if (is_specialized(c->launch.variant)) {
     if (ensure_gen(c, c->launch.block_threads, c->launch.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT) < 1) return -2;
   }
@@ -748,6 +798,7 @@ int pfchem_equilibrate_constraints(pfchem_ctx *c, pfchem_cells *cl, const pfchem
   if (!c || !cl || !con || !con->type || !con->value) return fail(c, -1, "null argument");
   if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
   if (!cl->on_device) return fail(c, -1, "pfchem_equilibrate_constraints takes device pointers");
+  if (c->net.act_newton) return fail(c, -1, "constraint speciation supports the LAG activity algorithm only");
   const DevNet &n = c->net;
   if (!cl->temperature || !cl->den_kg || !cl->pri_molal || !cl->ionic_strength || !cl->porosity || !cl->saturation ||
       !cl->volume)
@@ -820,6 +871,9 @@ int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
   if (!is_specialized(l->variant) && l->variant != PFCHEM_KERNEL_GENERIC)
     return fail(c, -1, "unknown kernel variant %d", l->variant);
   if (c->has_net) {
+    if (is_specialized(l->variant) && !specialized_supports(c->net))
+      return fail(c, -1, "the network-specialized kernel does not support the NEWTON activity algorithm at every "
+                         "Newton iteration");
     if (is_specialized(l->variant)) {
       const bool cmp = l->variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT;
       if (gen_shared_bytes(c->net, l->block_threads, cmp) > 227 * 1024)
@@ -846,6 +900,7 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   if (!cl->on_device) return fail(c, -1, "pfchem_autotune takes device pointers");
   cudaSetDevice(c->device);
   const DevNet &n = c->net;
+  if (!specialized_supports(n)) return 0;  // only the table-driven kernel applies: nothing to choose
   const int64_t nc = cl->ncells;
   // back up every array a solve writes, restore after each trial
   struct Arr {

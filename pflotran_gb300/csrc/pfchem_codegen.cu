@@ -134,6 +134,51 @@ struct Gen {
     return e;
   }
   bool act() const { return n.act_freq != PFCHEM_ACT_COEF_FREQUENCY_OFF; }
+  // rate prefactors: flat prefactor index of (mineral, prefactor), and the
+  // aqueous complexes some prefactor names (their log K term and activity
+  // coefficient are kept per cell)
+  int npf_total() const {
+    int t = 0;
+    for (int m = 0; m < n.Nm; ++m) t += n.mpn[m];
+    return t;
+  }
+  int pf_index(int mm, int p) const {
+    int t = 0;
+    for (int m = 0; m < mm; ++m) t += n.mpn[m];
+    return t + p;
+  }
+  std::vector<int> pf_complexes() const {
+    std::vector<int> v;
+    for (int m = 0; m < n.Nm; ++m)
+      for (int p = 0; p < n.mpn[m]; ++p)
+        for (int q = 0; q < n.mps[m][p]; ++q) {
+          const int id = n.mpid[m][p][q];
+          if (id < 0 && std::find(v.begin(), v.end(), -id - 1) == v.end()) v.push_back(-id - 1);
+        }
+    return v;
+  }
+  int pfc_slot(int i) const {
+    const auto v = pf_complexes();
+    return (int)(std::find(v.begin(), v.end(), i) - v.begin());
+  }
+  bool need_bk() const { return n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER; }
+  // log K term of complex i (for a prefactor's ln activity)
+  std::string pfK(int i) const { return need_bk() ? "L.bK[" + I(i) + "]" : "L.pK[" + I(pfc_slot(i)) + "]"; }
+  // activity coefficient of complex i
+  std::string pfg(int i) const {
+    return need_bk() ? "exp(L.bK[" + I(i) + "] - L.bc[" + I(i) + "])" : "L.pg[" + I(pfc_slot(i)) + "]";
+  }
+  // ln activity of prefactor species `id` (>= 0 primary, < 0 complex)
+  std::string pf_lnact(int id) const {
+    if (id >= 0) return "la" + I(id);
+    const int i = -id - 1;
+    std::string e = "(" + pfK(i);
+    for (int k = 0; k < n.cn[i]; ++k) {
+      const double nu = n.cnu[i][k];
+      e += " + " + (nu == 1.0 ? std::string("") : lit(nu) + " * ") + "la" + I(n.cid[i][k]);
+    }
+    return e + ")";
+  }
   // exact_jacobian_after: the Jacobian's exact terms are selected at run time
   bool rescue() const { return n.exact_after > 0 && !n.jac_exact; }
   // the exact-Jacobian condition as a C expression ("exact" at run time)
@@ -149,8 +194,11 @@ struct Gen {
   }
   bool need_tk() const {
     if (!n.isothermal) return true;
-    for (int k = 0; k < n.Nm; ++k)
+    for (int k = 0; k < n.Nm; ++k) {
       if (n.mEa[k] > 0.0) return true;
+      for (int p = 0; p < n.mpn[k]; ++p)
+        if (n.mpEa[k][p] > 0.0) return true;
+    }
     return false;
   }
   bool need_rho() const {
@@ -168,7 +216,9 @@ struct Gen {
     o << "#define NP " << n.N << "\n#define NC " << (n.Nc > 0 ? n.Nc : 1) << "\n#define NM "
       << (n.Nm > 0 ? n.Nm : 1) << "\n#define NIX " << (n.Nix > 0 ? n.Nix : 1) << "\n#define NSR "
       << (n.Nsr > 0 ? n.Nsr : 1) << "\n#define NSC " << (n.Nsc > 0 ? n.Nsc : 1) << "\n#define JS " << js << "\n"
-      << "#define NEED_BK " << (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? 1 : 0) << "\n";
+      << "#define NEED_BK " << (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? 1 : 0) << "\n"
+      << "#define NPF " << std::max(1, npf_total()) << "\n#define NPC " << std::max(1, (int)pf_complexes().size())
+      << "\n";
     o << R"(
 struct Lane {
   double m[NP], lm[NP], lg[NP], g[NP], fx[NP];
@@ -177,12 +227,13 @@ struct Lane {
   double bK[NC];
 #endif
   double bm[NM], rk[NM], vf[NM], ar[NM], rate[NM];
+  double pk[NPF], pK[NPC], pg[NPC];
   double bs[NSC];
   double ixr[NIX], srf[NSR];
   double P[NP], Sg[NP], F[NP], Sc[NP];
   double acc, psv_den, jac_aq, vol, v_t, den_L, dtc, por, rho_s, lnaw, tk, Icell, rplain, Iacc, Csum;
   int iter;
-  bool alt_pending, alt_used;
+  bool alt_pending, alt_used, act_fail;
 };
 __device__ __forceinline__ double sgn1(double x) { return signbit(x) ? -1.0 : 1.0; }
 __device__ __forceinline__ long long absbits(double x) { return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFLL; }
@@ -193,14 +244,20 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
 )";
   }
 
-  // LAG activity coefficients at ionic strength `Iv` (reaction.F90:3992-4051)
-  void activity(const char *Iv) {
+  // LAG activity coefficients at ionic strength `Iv` (reaction.F90:3992-4051);
+  // the complex constants are kbase[i] - ln gamma_i (kbase: the log K terms,
+  // by default the lane's own)
+  void activity(const char *Iv, const char *kbase = nullptr) {
     o << "  {\n  const double sI = sqrt(" << Iv << ");\n";
     bool needg[PFCHEM_MAX_PRI] = {};
     for (int r = 0; r < n.Nix; ++r)
       for (int k = 0; k < n.xn[r]; ++k) needg[n.xid[r][k]] = true;
     if (prod_any())
       for (int j = 0; j < n.N; ++j) needg[j] = true;
+    for (int m = 0; m < n.Nm; ++m)
+      for (int p = 0; p < n.mpn[m]; ++p)
+        for (int q = 0; q < n.mps[m][p]; ++q)
+          if (n.mpid[m][p][q] >= 0) needg[n.mpid[m][p][q]] = true;
     for (int j = 0; j < n.N; ++j) {
       if (n.Z2p[j] > 1e-20) {
         o << "  L.lg[" << j << "] = (" << lit(-n.Z2p[j] * n.A) << " * sI / (1.0 + " << lit(n.ap[j] * n.B)
@@ -212,13 +269,61 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       }
     }
     for (int i = 0; i < n.Nc; ++i) {
+      const std::string kb = kbase ? std::string(kbase) + "[" + I(i) + "]" : bK(i);
       if (n.cZ2[i] > 1e-20)
-        o << "  L.bc[" << i << "] = " << bK(i) << " - (" << lit(-n.cZ2[i] * n.A) << " * sI / (1.0 + "
+        o << "  L.bc[" << i << "] = " << kb << " - (" << lit(-n.cZ2[i] * n.A) << " * sI / (1.0 + "
           << lit(n.ca[i] * n.B) << " * sI) + " << lit(n.Bdot) << " * " << Iv << ") * " << lit(kLOG_TO_LN) << ";\n";
       else
-        o << "  L.bc[" << i << "] = " << bK(i) << ";\n";
+        o << "  L.bc[" << i << "] = " << kb << ";\n";
     }
     o << "  }\n";
+  }
+
+  // ACT_COEF_ALGORITHM_NEWTON at step start (reaction.F90:3846-3990): the
+  // ionic strength iterated to a 1e-6 relative change (at most 50 passes)
+  // with the primaries' ln activities held at their entry values (the
+  // coefficients at the carried ionic strength: the step's entry state at the
+  // library's boundary) and the complexes recomputed at every pass.
+  void activity_newton() {
+    o << "  { // NEWTON activity algorithm\n  double lk[NC];\n";
+    for (int i = 0; i < n.Nc; ++i) o << "  lk[" << i << "] = L.bc[" << i << "];\n";
+    activity("L.Icell", "lk");
+    for (int j = 0; j < n.N; ++j) o << "  const double lae" << j << " = L.lm[" << j << "] + L.lg[" << j << "];\n";
+    o << "  double sc[NC];\n  for (int i = 0; i < NC; ++i) sc[i] = 0.0;\n";
+    o << "  double fpri = 0.0;\n";
+    for (int j = 0; j < n.N; ++j)
+      if (n.Z2p[j] > 0) o << "  fpri = fpri + L.m[" << j << "] * " << lit(n.Z2p[j]) << ";\n";
+    o << "  double II = 0.0; int it = 0;\n  for (;;) {\n";
+    o << "    if (++it > 50) { L.act_fail = true; break; }\n    double I;\n";
+    o << "    if (it == 1) { I = L.Icell; } else {\n    I = fpri;\n";
+    for (int i = 0; i < n.Nc; ++i)
+      if (n.cZ2[i] > 0) o << "    I = I + sc[" << i << "] * " << lit(n.cZ2[i]) << ";\n";
+    o << "    I = 0.5 * I; }\n    const double f = I;\n    if (fabs(I - II) < 1e-6 * I) break;\n";
+    if (n.Nc > 0) {
+      o << "    { const double sI = sqrt(I); double didi = 0.0;\n";
+      for (int i = 0; i < n.Nc; ++i) {
+        if (!(n.cZ2[i] > 0)) continue;
+        o << "    { const double t = 1.0 + " << lit(n.B * n.ca[i]) << " * sI;\n";
+        o << "      double sum = " << lit(0.5 * n.A * n.cZ2[i]) << " / (sI * t * t) - " << lit(n.Bdot) << ";\n";
+        for (int k = 0; k < n.cn[i]; ++k) {
+          const int j = n.cid[i][k];
+          if (!(n.Z2p[j] > 0)) continue;
+          o << "      { const double tj = 1.0 + " << lit(n.B * n.ap[j]) << " * sI; sum = sum + " << lit(n.cnu[i][k])
+            << " * (" << lit(-0.5 * n.A * n.Z2p[j]) << " / (sI * tj * tj) + " << lit(n.Bdot) << "); }\n";
+        }
+        o << "      didi = didi + " << lit(0.5 * n.cZ2[i]) << " * (sc[" << i << "] * " << lit(kLOG_TO_LN) << " * sum); }\n";
+      }
+      o << "    const double den = 1.0 - didi;\n    II = fabs(den) > 0.0 ? (f - I * didi) / den : f; }\n";
+    } else {
+      o << "    II = f;\n";
+    }
+    activity("II", "lk");
+    for (int i = 0; i < n.Nc; ++i) {
+      o << "    { double s = L.bc[" << i << "];\n";
+      for (int k = 0; k < n.cn[i]; ++k) acc(o, "  s", n.cnu[i][k], "lae" + I(n.cid[i][k]));
+      o << "      sc[" << i << "] = exp(s); }\n";
+    }
+    o << "  }\n  }\n";
   }
 
   std::string logK(double iso, const double *coef) {
@@ -265,7 +370,17 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
         o << "  L.rk[" << k << "] = " << lit(n.mk[k]) << ";\n";
       o << "  L.vf[" << k << "] = a.vf[" << k << " * nc + cell]; L.ar[" << k << "] = a.area[" << k
         << " * nc + cell]; L.rate[" << k << "] = 0.0;\n";
+      for (int p = 0; p < n.mpn[k]; ++p) {
+        // a prefactor's rate constant with its own Arrhenius factor (reaction_mineral.F90:771-778)
+        if (n.mpEa[k][p] > 0.0)
+          o << "  L.pk[" << pf_index(k, p) << "] = " << lit(n.mpk[k][p]) << " * exp(" << lit(n.mpEa[k][p] / kIDEAL_GAS_CONSTANT)
+            << " * (" << lit(1.0 / (25.0 + 273.15)) << " - 1.0 / L.tk));\n";
+        else
+          o << "  L.pk[" << pf_index(k, p) << "] = " << lit(n.mpk[k][p]) << ";\n";
+      }
     }
+    if (!need_bk())
+      for (int i : pf_complexes()) o << "  L.pK[" << pfc_slot(i) << "] = L.bc[" << i << "];\n";
     for (int k = 0; k < n.Nsc; ++k) {
       o << "  L.bs[" << k << "] = " << logK(n.slogK[k], n.scoef[k]);
       if (n.sh2o[k] != 0.0) o << " + " << lit(n.sh2o[k]) << " * L.lnaw";
@@ -273,13 +388,17 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     }
     for (int r = 0; r < n.Nix; ++r) o << "  L.ixr[" << r << "] = a.ixref[" << r << " * nc + cell];\n";
     for (int r = 0; r < n.Nsr; ++r) o << "  L.srf[" << r << "] = a.srfree[" << r << " * nc + cell];\n";
-    o << "  L.Icell = a.ionic[cell];\n";
+    o << "  L.Icell = a.ionic[cell]; L.act_fail = false;\n";
     if (act()) {
-      activity("L.Icell");
+      if (n.act_newton) activity_newton();
+      else activity("L.Icell");
     } else {
       for (int j = 0; j < n.N; ++j) o << "  L.lg[" << j << "] = 0.0; L.g[" << j << "] = 1.0;\n";
       for (int i = 0; i < n.Nc; ++i) o << "  L.bc[" << i << "] = " << bK(i) << ";\n";
     }
+    if (!need_bk())
+      for (int i : pf_complexes())
+        o << "  L.pg[" << pfc_slot(i) << "] = exp(L.pK[" << pfc_slot(i) << "] - L.bc[" << i << "]);\n";
     // product-form constants: exp of the log constants, once per cell
     if (prod_mnrl())
       for (int k = 0; k < n.Nm; ++k) o << "  L.bm[" << k << "] = xexp(L.bm[" << k << "]);\n";
@@ -602,7 +721,31 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
       if (n.mthr[mm] > 0.0) o << "  if (sign_ < 0.0 && QK < " << lit(n.mthr[mm]) << ") on = false;\n";
       o << "  if (on) {\n";
       if (n.mlim[mm] > 0.0) o << "  aff = aff / (1.0 + (1.0 - aff) * " << lit(1.0 / n.mlim[mm]) << ");\n";
-      o << "  const double kr = L.rk[" << mm << "];\n";
+      if (n.mpn[mm] > 0) {
+        // rate prefactors (reaction_mineral.F90:743-782): a sum over parallel
+        // prefactors of products of Monod terms a^alpha / (1 + atten a^beta)
+        o << "  double kr = 0.0;\n";
+        for (int p = 0; p < n.mpn[mm]; ++p) {
+          o << "  double lp" << p << " = 0.0;\n";
+          for (int q = 0; q < n.mps[mm][p]; ++q) {
+            const double att = n.mpatt[mm][p][q];
+            o << "  double lps" << p << "_" << q << ";\n";
+            o << "  { const double lsa = " << pf_lnact(n.mpid[mm][p][q]) << ";\n";
+            o << "    const double lnum = " << lit(n.mpa[mm][p][q]) << " * lsa;\n";
+            if (att > 0.0)
+              o << "    const double lden = xlog(1.0 + xexp(" << lit(std::log(att)) << " + " << lit(n.mpb[mm][p][q])
+                << " * lsa));\n";
+            else
+              o << "    const double lden = 0.0;\n";
+            o << "    lp" << p << " = lp" << p << " + lnum; lp" << p << " = lp" << p << " - lden; lps" << p << "_" << q
+              << " = lnum - lden; }\n";
+          }
+          o << "  const double pf" << p << " = xexp(lp" << p << "); kr = kr + pf" << p << " * L.pk["
+            << pf_index(mm, p) << "];\n";
+        }
+      } else {
+        o << "  const double kr = L.rk[" << mm << "];\n";
+      }
       o << "  const double Imc = -L.ar[" << mm << "]" << (n.has_minscale ? " * " + lit(1.0 / n.mscale[mm]) : "") << ";\n";
       if (n.has_affpow) o << "  const double Im = Imc * sign_ * pow(fabs(aff), " << lit(n.mpow[mm]) << ") * kr;\n";
       else o << "  const double Im = Imc * sign_ * fabs(aff) * kr;\n";
@@ -637,6 +780,65 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
           o << "  }\n";
         }
         if (ex != "false") o << "  }\n";
+        if (n.mpn[mm] > 0) {
+          // derivative through the prefactors (reaction_mineral.F90:897-997)
+          // per ln m: a primary's column gets the mineral's stoichiometry times
+          // dIm/da * gamma * m; a complex's derivative goes through its
+          // components (dC/dln m_j = nu_j C) into the rows of the complex's
+          // species as RReact adds it, or (exact) into the mineral's rows
+          o << "  { const double dIm_dsum = ImV / kr;\n";
+          for (int p = 0; p < n.mpn[mm]; ++p) {
+            o << "  const double lpf" << p << " = xlog(pf" << p << ");\n";
+            for (int q = 0; q < n.mps[mm][p]; ++q) {
+              const int id = n.mpid[mm][p][q];
+              const double a_ = n.mpa[mm][p][q], b_ = n.mpb[mm][p][q], att = n.mpatt[mm][p][q];
+              const std::string ps = "lps" + I(p) + "_" + I(q);
+              o << "  { const double lsa = " << pf_lnact(id) << ";\n";
+              o << "    const double gs = " << (id >= 0 ? "L.g[" + I(id) + "]" : pfg(-id - 1)) << ";\n";
+              o << "    const double dpp = xexp(lpf" << p << " - " << ps << ");\n";
+              o << "    const double num = " << lit(a_) << " * xexp(" << ps << " - lsa);\n";
+              if (att > 0.0) {
+                o << "    const double lgb = " << lit(b_) << " * lsa;\n";
+                o << "    const double den = 1.0 + xexp(" << lit(std::log(att)) << " + lgb);\n";
+                o << "    const double dden = -1.0 * xexp(" << ps << ") / den * " << lit(att) << " * " << lit(b_)
+                  << " * xexp(lgb - lsa);\n";
+              } else {
+                o << "    const double dden = 0.0;\n";
+              }
+              o << "    const double dIm = dIm_dsum * dpp * ((num + dden) * gs) * L.pk[" << pf_index(mm, p) << "];\n";
+              if (id >= 0) {
+                o << "    { const double t = dIm * L.m[" << id << "];\n";
+                for (int k = 0; k < nz; ++k) acc(o, "    " + J(n.mid[mm][k], id), n.mnu[mm][k], "t");
+                o << "    }\n";
+              } else {
+                const int ci = -id - 1;
+                o << "    const double Ci = xexp(lsa) / gs;\n";
+                for (int jj = 0; jj < n.cn[ci]; ++jj) {
+                  const int j = n.cid[ci][jj];
+                  o << "    { const double t = " << times(n.cnu[ci][jj], "Ci") << " * dIm;\n";
+                  auto mineral_rows = [&]() {
+                    for (int k = 0; k < nz; ++k) acc(o, "      " + J(n.mid[mm][k], j), n.mnu[mm][k], "t");
+                  };
+                  auto complex_rows = [&]() {
+                    for (int k = 0; k < n.cn[ci]; ++k) acc(o, "      " + J(n.cid[ci][k], j), n.cnu[ci][k], "t");
+                  };
+                  if (ex == "true") mineral_rows();
+                  else if (ex == "false") complex_rows();
+                  else {
+                    o << "      if (" << ex << ") {\n";
+                    mineral_rows();
+                    o << "      } else {\n";
+                    complex_rows();
+                    o << "      }\n";
+                  }
+                  o << "    }\n";
+                }
+              }
+              o << "  }\n";
+            }
+          }
+          o << "  }\n";
+        }
       }
       o << "  }\n  }\n";
     }
@@ -773,6 +975,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     o << "__device__ __forceinline__ int newton_step(Lane &L, double *Jb, " << (compact ? "unsigned short" : "long long")
       << " *Eb) {\n";
     o << "  L.iter += 1;\n";
+    if (n.act_newton) o << "  if (L.act_fail) return " << PFCHEM_CELL_INNER_MAXITER << ";\n";
     if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER) {
       o << "  if (L.iter > 1) {\n  double Iv = L.Iacc;\n";
       for (int j = 0; j < N; ++j)
@@ -898,7 +1101,7 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   // whether the alternative guess was taken.
   int prep_fields() const {
     return 5 * n.N + n.Nc + (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER ? n.Nc : 0) + 2 * n.Nm + n.Nsc +
-           n.Nix + 1;
+           n.Nix + 1 + npf_total() + (need_bk() ? 0 : 2 * (int)pf_complexes().size());
   }
   void prep_io(bool store) {
     int f = 0;
@@ -919,8 +1122,16 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     for (int k = 0; k < n.Nm; ++k) fld("L.rk[" + I(k) + "]");
     for (int k = 0; k < n.Nsc; ++k) fld("L.bs[" + I(k) + "]");
     for (int r = 0; r < n.Nix; ++r) fld("L.ixr[" + I(r) + "]");
-    if (store) o << "  prep[" << f << " * nc + cell] = L.alt_used ? 1.0 : 0.0;\n";
-    else o << "  L.alt_used = prep[" << f << " * nc + cell] != 0.0;\n";
+    for (int t = 0; t < npf_total(); ++t) fld("L.pk[" + I(t) + "]");
+    if (!need_bk())
+      for (size_t q = 0; q < pf_complexes().size(); ++q) {
+        fld("L.pK[" + I((int)q) + "]");
+        fld("L.pg[" + I((int)q) + "]");
+      }
+    // flags: 1 = the alternative guess was taken, 2 = the activity algorithm failed
+    if (store) o << "  prep[" << f << " * nc + cell] = (L.alt_used ? 1.0 : 0.0) + (L.act_fail ? 2.0 : 0.0);\n";
+    else
+      o << "  { const double fl = prep[" << f << " * nc + cell]; L.alt_used = fl == 1.0 || fl == 3.0; L.act_fail = fl >= 2.0; }\n";
   }
 
   // Data-parallel prologue: one thread per cell, every lane busy.  It does

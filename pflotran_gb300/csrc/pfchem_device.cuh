@@ -26,6 +26,7 @@ struct DevNet {
   int32_t has_temkin, has_minscale, has_affpow, has_h2o_rxn;
   int32_t jac_exact;  // PFCHEM_JACOBIAN_EXACT
   int32_t exact_after;  // exact_jacobian_after (0: never)
+  int32_t act_newton;   // ACT_COEF_ALGORITHM_NEWTON
   double max_dlnC, rel_change_tol, res_tol;
   double A, B, Bdot;
   // primaries
@@ -45,6 +46,18 @@ struct DevNet {
   double mk[PFCHEM_MAX_MNRL], mEa[PFCHEM_MAX_MNRL], mVm[PFCHEM_MAX_MNRL];
   double mthr[PFCHEM_MAX_MNRL], mlim[PFCHEM_MAX_MNRL];
   double mtemkin[PFCHEM_MAX_MNRL], mscale[PFCHEM_MAX_MNRL], mpow[PFCHEM_MAX_MNRL];
+  // rate prefactors (reaction_mineral.F90:743-782): per mineral the number of
+  // prefactors; per prefactor its species count, rate constant and
+  // activation energy; per species its id (>= 0: primary, 0-based; < 0:
+  // aqueous complex -(i + 1)), alpha, beta and attenuation coefficient
+  int8_t mpn[PFCHEM_MAX_MNRL];
+  int8_t mps[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF];
+  int8_t mpid[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF][PFCHEM_MAX_PREF_SPEC];
+  double mpk[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF], mpEa[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF];
+  double mpa[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF][PFCHEM_MAX_PREF_SPEC];
+  double mpb[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF][PFCHEM_MAX_PREF_SPEC];
+  double mpatt[PFCHEM_MAX_MNRL][PFCHEM_MAX_PREF][PFCHEM_MAX_PREF_SPEC];
+  int32_t has_pref;
   // ion exchange
   int8_t xn[PFCHEM_MAX_IONX], xzflag[PFCHEM_MAX_IONX], xsurf[PFCHEM_MAX_IONX];
   int8_t xid[PFCHEM_MAX_IONX][PFCHEM_MAX_NNZ];

@@ -60,12 +60,14 @@ struct Lane {
   double fixed[S::NP], absfixed[S::NP];
   double bc[S::NCX], bK[S::NCX], C[S::NCX];
   double bm[S::NMN], rk[S::NMN], vf[S::NMN], area[S::NMN], rate[S::NMN];
+  double pk[S::NMN][PFCHEM_MAX_PREF];  // prefactor rate constant x Arrhenius factor
   double bs[S::NSC];
   double ixref[S::NIX], srfree[S::NSR];
   double Psi[S::NP], S_[S::NP], F[S::NP], Sc[S::NP];
   double I;
   int iter;
   bool alt_pending, alt_used;
+  bool act_fail;  // the NEWTON activity algorithm did not converge at step start
   double r_plain;
 };
 
@@ -90,6 +92,72 @@ __device__ void activity(const DevNet &n, Lane<S> &L, double I) {
       lg = (-n.cZ2[i] * sI * n.A / (1.0 + n.ca[i] * n.B * sI) + n.Bdot * I) * kLOG_TO_LN;
     L.bc[i] = L.bK[i] - lg;
   }
+}
+
+// ACT_COEF_ALGORITHM_NEWTON (reaction.F90:3846-3990): the ionic strength is
+// iterated to a 1e-6 relative change (at most 50 passes) with the primaries'
+// ln activities held at their entry values, the complexes recomputed at each
+// pass.  `entry` starts from the step's entry state at the library's
+// boundary: the primaries' coefficients at the carried ionic strength I0 and
+// no complexes (the first pass keeps I = I0).  Otherwise the entry state is
+// the lane's current coefficients and complexes (L.C, from the last
+// evaluation), as RActivityCoefficients sees them inside the Newton loop.
+// Returns 0, or 1 when the 50 passes did not converge.
+template <class S>
+__device__ int activity_newton(const DevNet &n, Lane<S> &L, bool entry, double I0) {
+  const int N = n.N;
+  if (entry) {
+    activity(n, L, I0);
+    for (int i = 0; i < n.Nc; ++i) L.C[i] = 0.0;
+  }
+  double lna[S::NP], fpri = 0.0;
+  for (int j = 0; j < N; ++j) {
+    lna[j] = L.lnm[j] + L.lngp[j];
+    fpri += L.m[j] * n.Z2p[j];
+  }
+  double II = 0.0;
+  for (int it = 1;; ++it) {
+    if (it > 50) return 1;
+    double I;
+    if (it == 1 && entry) {
+      I = I0;
+    } else {
+      I = fpri;
+      for (int i = 0; i < n.Nc; ++i) I += L.C[i] * n.cZ2[i];
+      I = 0.5 * I;
+    }
+    const double f = I;
+    if (fabs(I - II) < 1e-6 * I) break;
+    if (n.Nc > 0) {
+      double didi = 0.0;
+      const double sI = sqrt(I);
+      for (int i = 0; i < n.Nc; ++i) {
+        if (n.cZ2[i] > 0.0) {
+          const double t = 1.0 + n.B * n.ca[i] * sI;
+          double sum = 0.5 * n.A * n.cZ2[i] / (sI * t * t) - n.Bdot;
+          for (int k = 0; k < n.cn[i]; ++k) {
+            const int j = n.cid[i][k];
+            if (n.Z2p[j] > 0.0) {
+              const double tj = 1.0 + n.B * n.ap[j] * sI;
+              sum += n.cnu[i][k] * (-0.5 * n.A * n.Z2p[j] / (sI * tj * tj) + n.Bdot);
+            }
+          }
+          didi += 0.5 * n.cZ2[i] * (L.C[i] * kLOG_TO_LN * sum);
+        }
+      }
+      const double den = 1.0 - didi;
+      II = fabs(den) > 0.0 ? (f - I * didi) / den : f;
+    } else {
+      II = f;
+    }
+    activity(n, L, II);
+    for (int i = 0; i < n.Nc; ++i) {
+      double s = L.bc[i];
+      for (int k = 0; k < n.cn[i]; ++k) s += n.cnu[i][k] * lna[n.cid[i][k]];
+      L.C[i] = exp(s);
+    }
+  }
+  return 0;
 }
 
 __device__ __forceinline__ double logK_at(const double *c, double lntk, double tk, double itk) {
@@ -141,6 +209,12 @@ __device__ void setup(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> 
     double af = 1.0;  // Arrhenius factor (reaction_mineral.F90:784-792)
     if (n.mEa[k] > 0.0) af = exp(n.mEa[k] / kIDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (L.temp + 273.15)));
     L.rk[k] = n.mk[k] * af;
+    for (int p = 0; p < n.mpn[k]; ++p) {
+      double pf = 1.0;  // the prefactor's own Arrhenius factor (reaction_mineral.F90:771-778)
+      if (n.mpEa[k][p] > 0.0)
+        pf = exp(n.mpEa[k][p] / kIDEAL_GAS_CONSTANT * (1.0 / (25.0 + 273.15) - 1.0 / (L.temp + 273.15)));
+      L.pk[k][p] = n.mpk[k][p] * pf;
+    }
     L.vf[k] = a.vf[k * nc + cell];
     L.area[k] = a.area[k * nc + cell];
     L.rate[k] = 0.0;
@@ -152,8 +226,10 @@ __device__ void setup(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> 
   for (int r = 0; r < n.Nix; ++r) L.ixref[r] = a.ixref[r * nc + cell];
   for (int r = 0; r < n.Nsr; ++r) L.srfree[r] = a.srfree[r * nc + cell];
   L.I = a.ionic[cell];
+  L.act_fail = false;
   if (n.act_freq != PFCHEM_ACT_COEF_FREQUENCY_OFF) {
-    activity(n, L, L.I);
+    if (n.act_newton) L.act_fail = activity_newton(n, L, true, L.I) != 0;
+    else activity(n, L, L.I);
   } else {
     for (int j = 0; j < n.N; ++j) {
       L.lngp[j] = 0.0;
@@ -161,10 +237,21 @@ __device__ void setup(const DevNet &n, const CellArgs &a, int64_t cell, Lane<S> 
     }
     for (int i = 0; i < n.Nc; ++i) L.bc[i] = L.bK[i];
   }
-  for (int i = 0; i < n.Nc; ++i) L.C[i] = 0.0;
+  if (!n.act_newton) for (int i = 0; i < n.Nc; ++i) L.C[i] = 0.0;
   L.iter = 0;
   L.alt_pending = false;
   L.alt_used = false;
+}
+
+// ln activity of a rate-prefactor species: a primary (id >= 0) or an aqueous
+// complex -(id + 1), whose ln activity is its log K term plus sum nu ln a.
+template <class S>
+__device__ __forceinline__ double pref_lnact(const DevNet &n, const Lane<S> &L, const double *lna, int id) {
+  if (id >= 0) return lna[id];
+  const int i = -id - 1;
+  double s = L.bK[i];
+  for (int k = 0; k < n.cn[i]; ++k) s += n.cnu[i][k] * lna[n.cid[i][k]];
+  return s;
 }
 
 // Residual F (and, with JAC, the Jacobian dF/dln m into J, stride `js`) at
@@ -381,7 +468,27 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js, bool exa
     if (!(L.vf[mm] > 0.0 || sign_ < 0.0)) continue;
     if (n.mthr[mm] > 0.0 && sign_ < 0.0 && QK < n.mthr[mm]) continue;
     if (n.mlim[mm] > 0.0) aff = aff / (1.0 + (1.0 - aff) / n.mlim[mm]);
-    const double kr = L.rk[mm];
+    double kr = L.rk[mm];
+    // rate prefactors (reaction_mineral.F90:743-782): a sum over parallel
+    // prefactors of products of Monod terms a^alpha / (1 + atten a^beta)
+    const int npf = n.mpn[mm];
+    double pref[PFCHEM_MAX_PREF], lps[PFCHEM_MAX_PREF][PFCHEM_MAX_PREF_SPEC];
+    if (npf > 0) {
+      kr = 0.0;
+      for (int p = 0; p < npf; ++p) {
+        double lp = 0.0;
+        for (int q = 0; q < n.mps[mm][p]; ++q) {
+          const double lsa = pref_lnact(n, L, lna, n.mpid[mm][p][q]);
+          const double lnum = n.mpa[mm][p][q] * lsa;
+          const double lden = log(1.0 + exp(log(n.mpatt[mm][p][q]) + n.mpb[mm][p][q] * lsa));
+          lp = lp + lnum;
+          lp = lp - lden;
+          lps[p][q] = lnum - lden;
+        }
+        pref[p] = exp(lp);
+        kr = kr + pref[p] * L.pk[mm][p];
+      }
+    }
     double Imc = -L.area[mm];
     if (n.has_minscale) Imc = Imc / n.mscale[mm];
     double Im;
@@ -408,6 +515,44 @@ __device__ int evaluate(const DevNet &n, Lane<S> &L, double *J, int js, bool exa
         const int j = n.mid[mm][q];
         const double t = g * n.mnu[mm][q];
         for (int k = 0; k < nz; ++k) J[(n.mid[mm][k] * N + j) * js] += n.mnu[mm][k] * t;
+      }
+    }
+    if (JAC && npf > 0) {
+      // derivative through the prefactors (reaction_mineral.F90:897-997), per
+      // ln m: a primary's column gets the mineral's stoichiometry times
+      // dIm/da * gamma * m; a complex's derivative goes through its
+      // components (dC/dln m_j = nu_j C) into the rows of the complex's own
+      // species as RReact adds it, or (exact) into the mineral's rows
+      const double dIm_dsum = ImV / kr;
+      for (int p = 0; p < npf; ++p) {
+        const double lpf = log(pref[p]);
+        for (int q = 0; q < n.mps[mm][p]; ++q) {
+          const int id = n.mpid[mm][p][q];
+          const double lsa = pref_lnact(n, L, lna, id);
+          const double gs = id >= 0 ? L.gp[id] : exp(L.bK[-id - 1] - L.bc[-id - 1]);
+          const double a_ = n.mpa[mm][p][q], b_ = n.mpb[mm][p][q], att = n.mpatt[mm][p][q];
+          const double dpp = exp(lpf - lps[p][q]);
+          const double num = a_ * exp(lps[p][q] - lsa);
+          const double lgb = b_ * lsa;
+          const double den = 1.0 + exp(log(att) + lgb);
+          const double dden = -1.0 * exp(lps[p][q]) / den * att * b_ * exp(lgb - lsa);
+          const double dspec = (num + dden) * gs;
+          const double dIm = dIm_dsum * dpp * dspec * L.pk[mm][p] * L.jac_mnrl;
+          if (id >= 0) {
+            const double t = dIm * L.m[id];
+            for (int k = 0; k < nz; ++k) J[(n.mid[mm][k] * N + id) * js] += n.mnu[mm][k] * t;
+          } else {
+            const int ci = -id - 1;
+            for (int jj = 0; jj < n.cn[ci]; ++jj) {
+              const int j = n.cid[ci][jj];
+              const double t = n.cnu[ci][jj] * L.C[ci] * dIm;
+              if (exact)
+                for (int k = 0; k < nz; ++k) J[(n.mid[mm][k] * N + j) * js] += n.mnu[mm][k] * t;
+              else
+                for (int k = 0; k < n.cn[ci]; ++k) J[(n.cid[ci][k] * N + j) * js] += n.cnu[ci][k] * t;
+            }
+          }
+        }
       }
     }
   }
@@ -509,12 +654,17 @@ template <class S>
 __device__ int newton_step(const DevNet &n, Lane<S> &L, double *J, int js) {
   const int N = n.N;
   L.iter += 1;
+  if (L.act_fail) return PFCHEM_CELL_INNER_MAXITER;
   if (n.act_freq == PFCHEM_ACT_COEF_FREQUENCY_NEWTON_ITER && L.iter > 1) {
-    double I = 0.0;
-    for (int j = 0; j < N; ++j) I += L.m[j] * n.Z2p[j];
-    for (int i = 0; i < n.Nc; ++i) I += L.C[i] * n.cZ2[i];
-    I *= 0.5;
-    activity(n, L, I);
+    if (n.act_newton) {
+      if (activity_newton(n, L, false, 0.0)) return PFCHEM_CELL_INNER_MAXITER;
+    } else {
+      double I = 0.0;
+      for (int j = 0; j < N; ++j) I += L.m[j] * n.Z2p[j];
+      for (int i = 0; i < n.Nc; ++i) I += L.C[i] * n.cZ2[i];
+      I *= 0.5;
+      activity(n, L, I);
+    }
   }
   // past exact_jacobian_after iterations: the exact Jacobian, no damping
   const bool rescue = n.exact_after > 0 && L.iter > n.exact_after;

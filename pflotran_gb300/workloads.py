@@ -143,6 +143,28 @@ def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rh
     return net
 
 
+def add_rate_prefactors(net):
+    """Gives the first two kinetic minerals of `net` rate prefactors
+    (reaction_mineral.F90:743-782), in place, and rebuilds its tables:
+    mineral 0 a Monod term in the first primary (alpha 1, beta 1,
+    attenuation 1e4) plus a second parallel prefactor in the first aqueous
+    complex (alpha 0.5, beta 1, attenuation 10) and the third primary
+    (alpha 1, no attenuation) with its own activation energy; mineral 1 one
+    prefactor in the second primary (alpha 0.5, beta 0.5, attenuation 100).
+    Returns net."""
+    pn = net.pri_names
+    cx = net.complexes[0].extra["name"]
+    m0, m1 = net.minerals[0], net.minerals[min(1, len(net.minerals) - 1)]
+    k0, k1 = m0.extra["k"], m1.extra["k"]
+    m0.extra["pref"] = [dict(rate=10.0 * k0, species=[(pn[0], 1.0, 1.0, 1e4)]),
+                        dict(rate=k0, Ea=3e4, species=[(cx, 0.5, 1.0, 10.0), (pn[2 % len(pn)], 1.0, 0.0, 0.0)])]
+    if m1 is not m0:
+        m1.extra["pref"] = [dict(rate=k1, species=[(pn[1 % len(pn)], 0.5, 0.5, 100.0)])]
+    net._tables = None
+    net.build()
+    return net
+
+
 # ---------------------------------------------------------------------------
 # forward speciation for input generation (torch, float64, CPU or CUDA)
 

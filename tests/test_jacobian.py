@@ -103,3 +103,22 @@ def test_reaction_blocks_are_derivatives(oracle):
         # the reference's aqueous block is exact, its sorbed and reaction blocks are not
         assert rel(br["dtotal"][0].T, bx["dtotal"][0].T) < 1e-12
         np.testing.assert_array_equal(br["res"], bx["res"])
+
+
+def test_exact_jacobian_is_the_derivative_with_rate_prefactors(oracle):
+    """Minerals with rate prefactors (Monod terms in primaries and in an
+    aqueous complex, a prefactor with its own activation energy,
+    reaction_mineral.F90:743-782): the exact option's Jacobian, including
+    the prefactor terms of :897-997, is the derivative of the residual."""
+    net, opt, cells, dt = workloads.synthetic_cells(30, seed=24)
+    workloads.add_rate_prefactors(net)
+    sol = cells.copy()
+    oracle.react(net.as_struct(), opt, dt, sol, 0, 4)
+    exact = workloads.default_options(use_isothermal=1, jacobian=abi.JACOBIAN_EXACT)
+    rho = []
+    for k in range(cells.ncells):
+        if sol.status[k] != 0:
+            continue
+        m = sol.pri_molal.reshape(net.N, -1)[:, k].copy()
+        rho.append(_fd_contraction(oracle, net, exact, cells, dt, k, m))
+    assert len(rho) >= 25 and max(rho) < 1e-5, max(rho)

@@ -185,10 +185,49 @@ def test_rejects_unsupported_networks():
     with pytest.raises(PfchemError, match="naqcomp"):
         ReactionStep(net, default_options())
     net = workloads.calcite_network()
-    net.minerals[0].extra["pref"] = [dict(rate=1e-9, species=[("H+", 1.0, 0.0, 1.0)])]
+    net.minerals[0].extra["pref"] = [dict(rate=1e-9, species=[("H+", 1.0, 0.0, -1.0)])]
     net.build()
-    with pytest.raises(PfchemError, match="prefactors"):
+    with pytest.raises(PfchemError, match="attenuation"):
         ReactionStep(net, default_options())
+
+
+@pytest.mark.parametrize("kind", ["calcite_grid", "synthetic"])
+@pytest.mark.parametrize("jacobian", [abi.JACOBIAN_REFERENCE, abi.JACOBIAN_EXACT])
+@pytest.mark.parametrize("variant", [abi.KERNEL_SPECIALIZED, abi.KERNEL_GENERIC])
+def test_mineral_rate_prefactors(oracle, kind, jacobian, variant):
+    """Minerals with rate prefactors (reaction_mineral.F90:743-782 rate,
+    :897-997 Jacobian): Monod terms in primaries and in an aqueous complex,
+    parallel prefactors, a prefactor with its own activation energy (the
+    calcite grid is temperature-dependent).  Both kernels, both Jacobians,
+    against the oracle: 1e-10 on cells whose iteration counts agree, the
+    per-cell bar against the root elsewhere."""
+    from oracle import parity
+    if kind == "calcite_grid":
+        net, opt, cells, dt = workloads.calcite_cells(4096, seed=31, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(4096, seed=32)
+    workloads.add_rate_prefactors(net)
+    opt.jacobian = jacobian
+    ref = parity.solve(net, opt, dt, cells)
+    step = ReactionStep(net, opt)
+    if variant == abi.KERNEL_GENERIC:
+        step.set_launch(64, 1, 8, abi.KERNEL_GENERIC)
+    d = cells.to_device()
+    d.sec_molal = None
+    step.react(d, dt)
+    gpu = d.to_host()
+    ok = (ref.status == 0) & (gpu.status == 0)
+    assert ok.all(), (np.bincount(ref.status), np.bincount(gpu.status))
+    same = ref.iterations == gpu.iterations
+    assert same.mean() > 0.98
+    gpu.sec_molal = None
+    ref.sec_molal = None
+    assert_parity(net, gpu, ref, mask=same)
+    rates = ref.mnrl_rate.reshape(-1, cells.ncells)[:net.Nm]
+    assert (np.abs(rates) > 0).any()
+    truth = parity.truth_solve(net, opt, dt, cells, ref)
+    for q, (bar, *_r) in parity.per_cell_bar(net, gpu, ref, truth).items():
+        assert bar.all(), (q, int((~bar).sum()))
 
 
 def test_calcite_grid_full_size_sampled(oracle):
@@ -465,3 +504,46 @@ def test_network_from_database_in_a_swapped_basis(oracle, tmp_path):
     ref, gpu, _ = run_both(oracle, b, opt, cb, dt)
     assert (ref.status == 0).all() and (gpu.status == 0).all()
     assert_parity(b, gpu, ref)
+
+
+@pytest.mark.parametrize("kind", ["calcite_grid", "synthetic"])
+@pytest.mark.parametrize("mode", ["timestep_specialized", "timestep_generic", "newton_iter"])
+def test_newton_activity_algorithm(oracle, kind, mode):
+    """ACT_COEF_ALGORITHM_NEWTON (reaction.F90:3846-3990): the ionic
+    strength iterated with the primaries' entry activities held, at step
+    start (TIMESTEP: network-specialized and table-driven kernels) or at
+    every Newton iteration (NEWTON_ITER: the table-driven kernel, which the
+    library selects for it).  Against the oracle at 1e-10 on cells whose
+    iteration counts agree, the per-cell bar against the root elsewhere;
+    cells whose activity loop exceeds its 50 passes report the same status."""
+    from oracle import parity
+    if kind == "calcite_grid":
+        net, opt, cells, dt = workloads.calcite_cells(4096, seed=33, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(4096, seed=34)
+    opt.act_coef_update_algorithm = abi.ACT_COEF_ALGORITHM_NEWTON
+    opt.act_coef_update_frequency = (abi.ACT_COEF_FREQUENCY_NEWTON_ITER if mode == "newton_iter"
+                                     else abi.ACT_COEF_FREQUENCY_TIMESTEP)
+    ref = parity.solve(net, opt, dt, cells)
+    step = ReactionStep(net, opt)
+    if mode == "timestep_generic":
+        step.set_launch(64, 1, 8, abi.KERNEL_GENERIC)
+    if mode == "newton_iter":
+        assert step.launch().variant == abi.KERNEL_GENERIC
+        with pytest.raises(PfchemError, match="NEWTON activity"):
+            step.set_launch(32, 1, 1, abi.KERNEL_SPECIALIZED)
+    d = cells.to_device()
+    d.sec_molal = None
+    step.react(d, dt)
+    gpu = d.to_host()
+    ok = (ref.status == 0) & (gpu.status == 0)
+    assert ok.mean() > 0.99
+    assert np.mean(ref.status == gpu.status) > 0.999
+    same = ok & (ref.iterations == gpu.iterations)
+    assert same.sum() > 0.98 * ok.sum()
+    gpu.sec_molal = None
+    ref.sec_molal = None
+    assert_parity(net, gpu, ref, mask=same)
+    truth = parity.truth_solve(net, opt, dt, cells, ref)
+    for q, (bar, *_r) in parity.per_cell_bar(net, gpu, ref, truth, mask=ok & (truth.status == 0)).items():
+        assert bar.all(), (q, int((~bar).sum()))
