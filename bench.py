@@ -421,8 +421,22 @@ def main():
             pidx = sample_indices(n, args.cpu_sample)
             pred_sample = pred[:, torch.as_tensor(pidx, device=pred.device)].cpu().numpy().copy()
         del pred
+        # inference alone: features + the fused four-layer MLP (+ weight
+        # packing and the guess copy) over all cells, best of 3 synchronous calls
+        inf_ms = []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            g_ = step.surrogate_predict(dev)
+            inf_ms.append((time.perf_counter() - t0) * 1e3)
+            del g_
+        inf_flops = 2.0 * (16 * 256 + 2 * 256 * 256 + 256 * 16) * n
+        inference = {"ms": min(inf_ms), "tflops": inf_flops / (min(inf_ms) * 1e-3) / 1e12,
+                     "flops": inf_flops,
+                     "frac_of_bf16_peak": inf_flops / (min(inf_ms) * 1e-3) / 1e12 / _bf16_peak(),
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}
         step.surrogate_enable(True)
-        warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit,
+        warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit, inference=inference,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),
                     err0_rms=float(err0.pow(2).mean().sqrt()), err0_p50=float(err0.max(0).values.median()))
         del err, err0, sol, plain_guess
@@ -446,6 +460,7 @@ def main():
         if warm is not None:
             step.surrogate_enable(True)
     exact = None
+    exact_out = {}
     if args.exact_jacobian:
         # the same step with the exact Newton Jacobian (same equations and root)
         from pflotran_gb300 import abi
@@ -456,6 +471,7 @@ def main():
                 step.surrogate_enable(mode == "warm")
             r = timed(local)
             ge = dev.to_host()
+            exact_out[mode] = ge
             exact[mode] = {"value": r["value"], "ms_per_step": r["total_ms"] / args.steps,
                            "mean_newton_iterations": float(np.mean(r["iters"])) / n,
                            "max_newton_iterations": int(ge.iterations.max()),
@@ -463,6 +479,10 @@ def main():
                            "nonconverged": r["nonconverged"]}
         if warm is not None:
             exact["speedup_warm_vs_plain"] = exact["warm"]["value"] / exact["plain"]["value"]
+            # the learned warm start with exact Newton against the plain
+            # RReact Newton (reference Jacobian): both within the per-cell bar
+            # of the reference (parity.exact_warm_vs_reference_oracle)
+            exact["speedup_warm_exact_vs_plain_reference"] = exact["warm"]["value"] / plain["value"]
         step.set_options(opt)
         if warm is not None:
             step.surrogate_enable(True)
@@ -538,7 +558,8 @@ def main():
                                "train_ms_device": r.train_ms, "data_generation_s": warm["t_gen"],
                                "ln_m_error_rms": warm["err_rms"], "ln_m_maxerr_median": warm["err_p50"],
                                "plain_guess_ln_m_error_rms": warm["err0_rms"],
-                               "plain_guess_ln_m_maxerr_median": warm["err0_p50"]}}
+                               "plain_guess_ln_m_maxerr_median": warm["err0_p50"],
+                               "inference": warm["inference"]}}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
@@ -597,6 +618,10 @@ def main():
             par["warm"] = parity_block(net, opt, dt, sub, ref_w, g.subset(idx, net), truth)
             both = (ref.status == 0) & (g.subset(idx, net).status == 0)
             par["warm_vs_plain_oracle"] = parity.error_statement(net, g.subset(idx, net), ref, both)
+        for mode, ge in exact_out.items():
+            # the exact-Jacobian solves against the oracle's RReact (reference
+            # Jacobian, same options otherwise): the per-cell bar
+            par[f"exact_{mode}_vs_reference_oracle"] = parity_block(net, opt, dt, sub, ref, ge.subset(idx, net), truth)
         line["parity"] = par
         if g_ref is not None:
             # RReact's damped path: the cells the 200-iteration cap stops,
@@ -622,6 +647,13 @@ def main():
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def _bf16_peak():
+    try:
+        return float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["bf16_tflops"])
+    except Exception:
+        return 1910.0
 
 
 def fp64_peak(device):

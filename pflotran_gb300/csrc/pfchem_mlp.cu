@@ -61,17 +61,71 @@ __device__ __forceinline__ void mma16816(float *c, const uint32_t *a, const uint
 enum { kEpiAct = 0, kEpiF32 = 1 };
 constexpr int BM = 64, BN = 64, BK = 32, PAD = 8;
 
+__device__ __forceinline__ bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// One BR x BK tile of a strided BF16 operand X(r, k) = X[r*sr + k*sk] into
+// T[r][k] (k contiguous in shared memory).  When one stride is 1 the global
+// loads are 16-byte vectors along it (8 elements): along k they land in one
+// shared-memory row, along r they are scattered down a column.  Out-of-range
+// elements are zero.
+template <int BR>
+__device__ __forceinline__ void load_tile(bf16 (*T)[BK + PAD], const bf16 *__restrict__ X, long long sr, long long sk,
+                                          int R, int K, int r0, int k0, int tid) {
+  const bf16 zero = __float2bfloat16(0.f);
+  if (sk == 1) {
+    for (int e = tid; e < BR * BK / 8; e += 128) {
+      const int rr = e / (BK / 8), kk = (e % (BK / 8)) * 8;
+      const int gr = r0 + rr, gk = k0 + kk;
+      const bf16 *src = X + (long long)gr * sr + gk;
+      if (gr < R && gk + 8 <= K && aligned16(src)) {
+        *reinterpret_cast<uint4 *>(&T[rr][kk]) = *reinterpret_cast<const uint4 *>(src);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) T[rr][kk + q] = (gr < R && gk + q < K) ? src[q] : zero;
+      }
+    }
+  } else if (sr == 1) {
+    for (int e = tid; e < BR * BK / 8; e += 128) {
+      const int kk = e / (BR / 8), rr = (e % (BR / 8)) * 8;
+      const int gr = r0 + rr, gk = k0 + kk;
+      const bf16 *src = X + (long long)gk * sk + gr;
+      if (gk < K && gr + 8 <= R && aligned16(src)) {
+        uint4 v = *reinterpret_cast<const uint4 *>(src);
+        const bf16 *h = reinterpret_cast<const bf16 *>(&v);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) T[rr + q][kk] = h[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) T[rr + q][kk] = (gk < K && gr + q < R) ? src[q] : zero;
+      }
+    }
+  } else {
+    for (int e = tid; e < BR * BK; e += 128) {
+      const int rr = e / BK, kk = e % BK;
+      const int gr = r0 + rr, gk = k0 + kk;
+      T[rr][kk] = (gr < R && gk < K) ? X[(long long)gr * sr + (long long)gk * sk] : zero;
+    }
+  }
+}
+
+// C(m, n) = sum_k A(m, k) B(k, n), A(m, k) = A[m*sam + k*sak], B(k, n) = B[k*sbk + n*sbn].
+// Epilogues: kEpiAct: Cf = acc + bias (FP32), Cb = act(acc + bias) (BF16);
+//            kEpiF32: Cf = acc (+ bias).
+// Split K: block z sums k in [z*kchunk, (z+1)*kchunk) and, with more than
+// one split, writes its partial product to Cf + z*M*ldc (no bias); the
+// partials are then summed in a fixed order by sum_splits.
 template <int EPI>
 __global__ void __launch_bounds__(128) gemm_bf16(const bf16 *__restrict__ A, long long sam, long long sak,
                                                   const bf16 *__restrict__ B, long long sbk, long long sbn, int M,
                                                   int N, int K, const float *__restrict__ bias, float *Cf, bf16 *Cb,
-                                                  int ldc, int act) {
+                                                  int ldc, int act, int kchunk) {
   __shared__ __align__(16) bf16 As[BM][BK + PAD];
   __shared__ __align__(16) bf16 Bs[BN][BK + PAD];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int wm = warp >> 1, wn = warp & 1;
   const int g = lane >> 2, t = lane & 3;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int kb = blockIdx.z * kchunk, ke = min(K, kb + kchunk);
   float acc[2][4][4];
 #pragma unroll
   for (int i = 0; i < 2; ++i)
@@ -79,18 +133,9 @@ __global__ void __launch_bounds__(128) gemm_bf16(const bf16 *__restrict__ A, lon
     for (int j = 0; j < 4; ++j)
 #pragma unroll
       for (int q = 0; q < 4; ++q) acc[i][j][q] = 0.f;
-  const bf16 zero = __float2bfloat16(0.f);
-  for (int k0 = 0; k0 < K; k0 += BK) {
-    for (int e = tid; e < BM * BK; e += 128) {
-      const int mm = e / BK, kk = e % BK;
-      const int gm = m0 + mm, gk = k0 + kk;
-      As[mm][kk] = (gm < M && gk < K) ? A[(long long)gm * sam + (long long)gk * sak] : zero;
-    }
-    for (int e = tid; e < BN * BK; e += 128) {
-      const int nn = e / BK, kk = e % BK;
-      const int gn = n0 + nn, gk = k0 + kk;
-      Bs[nn][kk] = (gn < N && gk < K) ? B[(long long)gk * sbk + (long long)gn * sbn] : zero;
-    }
+  for (int k0 = kb; k0 < ke; k0 += BK) {
+    load_tile<BM>(As, A, sam, sak, M, ke, m0, k0, tid);
+    load_tile<BN>(Bs, B, sbn, sbk, N, ke, n0, k0, tid);
     __syncthreads();
 #pragma unroll
     for (int ks = 0; ks < BK; ks += 16) {
@@ -116,6 +161,8 @@ __global__ void __launch_bounds__(128) gemm_bf16(const bf16 *__restrict__ A, lon
     }
     __syncthreads();
   }
+  const bool split = gridDim.z > 1;
+  float *Co = split ? Cf + (long long)blockIdx.z * M * ldc : Cf;
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -125,16 +172,25 @@ __global__ void __launch_bounds__(128) gemm_bf16(const bf16 *__restrict__ A, lon
         const int r = m0 + wm * 32 + i * 16 + g + (q >= 2 ? 8 : 0);
         const int c = n0 + wn * 32 + j * 8 + 2 * t + (q & 1);
         if (r < M && c < N) {
-          float z = acc[i][j][q] + (bias ? bias[c] : 0.f);
+          float z = acc[i][j][q] + ((bias && !split) ? bias[c] : 0.f);
           const long long o = (long long)r * ldc + c;
           if (EPI == kEpiAct) {
             if (Cf) Cf[o] = z;
             Cb[o] = __float2bfloat16(act ? gelu(z) : z);
           } else {
-            Cf[o] = z;
+            Co[o] = z;
           }
         }
       }
+}
+
+// out[i] = sum over the splits of part[z][i], in split order
+__global__ void sum_splits(const float *__restrict__ part, float *out, long long n, int splits) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float s = 0.f;
+  for (int z = 0; z < splits; ++z) s += part[(long long)z * n + i];
+  out[i] = s;
 }
 
 // dZ = dH * GELU'(Z), dH given in FP32; output BF16 (GEMM operand) and FP32 kept
@@ -409,7 +465,21 @@ template <int EPI>
 void gemm(cudaStream_t st, const bf16 *A, long long sam, long long sak, const bf16 *B, long long sbk, long long sbn,
           int M, int N, int K, const float *bias, float *Cf, bf16 *Cb, int ldc, int act) {
   dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM);
-  gemm_bf16<EPI><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, bias, Cf, Cb, ldc, act);
+  gemm_bf16<EPI><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, bias, Cf, Cb, ldc, act, K);
+}
+
+// C = A B over a long K (the weight gradients: K = the batch rows) split
+// into `splits` slices of whole BK tiles, partials in `ws` (splits x M x N
+// floats), summed in a fixed order into C (ldc = N).
+void gemm_split_k(cudaStream_t st, const bf16 *A, long long sam, long long sak, const bf16 *B, long long sbk,
+                  long long sbn, int M, int N, int K, float *C, float *ws, int splits) {
+  int kchunk = (K + splits - 1) / splits;
+  kchunk = (kchunk + BK - 1) / BK * BK;
+  splits = (K + kchunk - 1) / kchunk;
+  dim3 grid((N + BN - 1) / BN, (M + BM - 1) / BM, splits);
+  gemm_bf16<kEpiF32><<<grid, 128, 0, st>>>(A, sam, sak, B, sbk, sbn, M, N, K, nullptr, splits > 1 ? ws : C, nullptr,
+                                           N, 0, kchunk);
+  if (splits > 1) sum_splits<<<blocks((long long)M * N, 256), 256, 0, st>>>(ws, C, (long long)M * N, splits);
 }
 
 }  // namespace
@@ -434,7 +504,9 @@ struct Surrogate {
   long long guess_cap = 0;
   int steps = 0;
   uint32_t *wpk = nullptr;  // B-fragment packing of the BF16 weights (fused inference)
+  float *ws = nullptr;      // split-K partials of the weight gradients (kSplits x 256 x 256)
 };
+constexpr int kSplits = 16;  // weight-gradient GEMMs: K = batch rows split 16 ways
 
 namespace {
 void free_acts(Surrogate *s) {
@@ -501,7 +573,7 @@ void backward(Surrogate *s, long long rows, cudaStream_t st) {
     const bf16 *dZb = s->db[l];
     const float *dZf = (l == kLayers - 1) ? s->dy : s->dz[l];
     // dW[K x N] = inp^T [K x rows] . dZ [rows x N]
-    gemm<kEpiF32>(st, inp, 1, K, dZb, Nn, 1, K, Nn, (int)rows, nullptr, s->grad + s->woff[l], nullptr, Nn, 0);
+    gemm_split_k(st, inp, 1, K, dZb, Nn, 1, K, Nn, (int)rows, s->grad + s->woff[l], s->ws, kSplits);
     // db = column sums of dZ
     bias_grad<<<dim3(blocks(Nn, 128), 64), 128, 0, st>>>(dZf, s->grad + s->boff[l], (int)rows, Nn);
     if (l > 0) {
