@@ -403,6 +403,15 @@ typedef struct pfchem_launch {
 #define PFCHEM_KERNEL_GENERIC 1     /* table-driven kernel compiled into the library */
 #define PFCHEM_KERNEL_SPECIALIZED_COMPACT 2 /* specialized, J alone in shared memory (right-hand
                                                side in registers): fits more blocks per SM, same results */
+/* Cooperative kernels: 8, 16 or 32 lanes solve one cell together (species,
+ * complexes, Jacobian entries, sorption sites, minerals and LU rows spread
+ * over the lanes; the cell's system in shared memory once per group).  Not
+ * for the linear update, the NEWTON activity algorithm or the activity of
+ * water.  block_threads: a multiple of 32 (128 recommended);
+ * refill_min_idle: unused. */
+#define PFCHEM_KERNEL_COOP8 3
+#define PFCHEM_KERNEL_COOP16 4
+#define PFCHEM_KERNEL_COOP32 5
 int pfchem_get_launch(const pfchem_ctx *ctx, pfchem_launch *launch);
 int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
 /* Times candidate mappings on `cells` (device pointers; the state arrays are
@@ -410,9 +419,12 @@ int pfchem_set_launch(pfchem_ctx *ctx, const pfchem_launch *launch);
  * block, the augmented or the compact shared-memory layout of the
  * network-specialized kernel (the candidates compiled concurrently), as many
  * resident blocks per SM as fit or one fewer, and a refill at 1, 2, 4 or 8
- * idle lanes; each candidate runs twice and its faster run counts.  Every
- * candidate computes each cell with the same operations, so the answers do
- * not depend on the choice. */
+ * idle lanes; then the cooperative kernels with 8, 16 and 32 lanes per cell
+ * (128-thread blocks, as many or one fewer per SM).  Each candidate runs
+ * twice and its faster run counts.  The specialized candidates compute each
+ * cell with the same operations (the same answers whichever is chosen); a
+ * cooperative kernel sums some terms in another order (answers equal to
+ * rounding). */
 int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
 
 /* ---------------------------------------------------------------------------

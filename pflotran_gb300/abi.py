@@ -41,6 +41,9 @@ CELL_INACTIVE = 5
 KERNEL_SPECIALIZED = 0
 KERNEL_GENERIC = 1
 KERNEL_SPECIALIZED_COMPACT = 2
+KERNEL_COOP8 = 3
+KERNEL_COOP16 = 4
+KERNEL_COOP32 = 5
 JACOBIAN_REFERENCE = 0
 JACOBIAN_EXACT = 1
 

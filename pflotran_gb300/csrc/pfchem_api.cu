@@ -38,6 +38,14 @@ size_t gen_shared_bytes(const DevNet &n, int block, bool compact);
 std::string generate_source(const DevNet &n, int block, bool compact);
 cudaError_t gen_launch(void *fn, void *pro, const DevNet &n, const CellArgs &a, Scratch *scr, double *prep, int grid,
                        int block, int refill, cudaStream_t st, bool compact);
+bool coop_supports(const DevNet &n);
+int coop_group_doubles(const DevNet &n);
+size_t coop_tables_bytes();
+struct CoopTables;
+void coop_build_tables(const DevNet &n, CoopTables *t);
+cudaError_t coop_launch(int lanes, const DevNet &n, const CellArgs &a, const void *tables, Scratch *scr, int grid,
+                        int block, cudaStream_t st);
+int coop_blocks_per_sm(int lanes, const DevNet &n, int block);
 struct Surrogate;
 Surrogate *surrogate_create(int N, uint64_t seed, std::string *err);
 void surrogate_destroy(Surrogate *s);
@@ -93,6 +101,7 @@ struct pfchem_ctx {
   bool gen_compact = false;  // its shared-memory layout (PFCHEM_KERNEL_SPECIALIZED_COMPACT)
   double *prep = nullptr;  // prologue records, gen_prep_fields x prep_cells doubles
   int64_t prep_cells = 0;
+  void *coop_tables = nullptr;  // gather lists of the cooperative kernels (device)
   Surrogate *sur = nullptr;  // learned warm start
   bool sur_on = false;
   int64_t async_cells = 0;  // cells of the last pfchem_react_batch_async
@@ -333,6 +342,8 @@ void default_launch(pfchem_ctx *c) {
 // Compiles (or reuses) the network-specialized kernel for `block` threads per
 // block and returns its resident blocks per SM (0 on failure, message in err).
 bool is_specialized(int v) { return v == PFCHEM_KERNEL_SPECIALIZED || v == PFCHEM_KERNEL_SPECIALIZED_COMPACT; }
+bool is_coop(int v) { return v == PFCHEM_KERNEL_COOP8 || v == PFCHEM_KERNEL_COOP16 || v == PFCHEM_KERNEL_COOP32; }
+int coop_lanes(int v) { return v == PFCHEM_KERNEL_COOP8 ? 8 : v == PFCHEM_KERNEL_COOP16 ? 16 : 32; }
 
 // The network-specialized kernel covers every option but the NEWTON activity
 // algorithm updated at every Newton iteration, which needs each complex's
@@ -469,6 +480,8 @@ int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st
   cudaError_t le = is_specialized(L.variant)
                        ? gen_launch(c->gen_fn, c->gen_pro, n, a, scr, prep, grid, L.block_threads,
                                     L.refill_min_idle, st, L.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT)
+                   : is_coop(L.variant)
+                       ? coop_launch(coop_lanes(L.variant), n, a, c->coop_tables, scr, grid, L.block_threads, st)
                        : launch_react(n, a, scr, grid, L.block_threads, L.refill_min_idle, st);
   if (le != cudaSuccess) return fail(c, -2, "solve launch: %s", cudaGetErrorString(le));
   return 0;
@@ -642,6 +655,7 @@ void pfchem_destroy(pfchem_ctx *c) {
   if (c->graph) cudaGraphExecDestroy(c->graph);
   if (c->sur) surrogate_destroy(c->sur);
   if (c->prep) cudaFree(c->prep);
+  if (c->coop_tables) cudaFree(c->coop_tables);
   for (auto &b : c->stage)
     if (b.ptr) cudaFree(b.ptr);
   if (c->scratch) cudaFree(c->scratch);
@@ -659,6 +673,13 @@ int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_op
   DevNet n;
   int e = build_devnet(c, net, opt, n);
   if (e) return e;
+  // gather lists of the cooperative kernels
+  {
+    std::vector<char> h(coop_tables_bytes());
+    coop_build_tables(n, reinterpret_cast<CoopTables *>(h.data()));
+    if (!c->coop_tables) CUDA_TRY(c, cudaMalloc(&c->coop_tables, h.size()));
+    CUDA_TRY(c, cudaMemcpy(c->coop_tables, h.data(), h.size(), cudaMemcpyHostToDevice));
+  }
   c->net = n;
   c->opt = *opt;
   c->has_net = true;
@@ -673,6 +694,9 @@ int pfchem_set_network(pfchem_ctx *c, const pfchem_network *net, const pfchem_op
     // error); the table-driven kernel where the specialized one does not apply
     default_launch(c);
     if (specialized_supports(n) && default_specialized_launch(c) != 0) return -2;
+  } else if (is_coop(c->launch.variant) && !coop_supports(n)) {
+    return fail(c, -1, "the cooperative kernels do not support these options (linear update, NEWTON activity "
+                       "algorithm or activity of water); set another launch");
   } else if (is_specialized(c->launch.variant) && !specialized_supports(n)) {
     return fail(c, -1, "the network-specialized kernel does not support the NEWTON activity algorithm at every "
                        "Newton iteration; set a PFCHEM_KERNEL_GENERIC launch");
@@ -868,8 +892,19 @@ int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
     return fail(c, -1, "block_threads must be a multiple of 32 in [32, 256]");
   if (l->refill_min_idle < 1 || l->refill_min_idle > 32) return fail(c, -1, "refill_min_idle must be in [1, 32]");
   if (l->blocks_per_sm < 1) return fail(c, -1, "blocks_per_sm must be >= 1");
-  if (!is_specialized(l->variant) && l->variant != PFCHEM_KERNEL_GENERIC)
+  if (!is_specialized(l->variant) && !is_coop(l->variant) && l->variant != PFCHEM_KERNEL_GENERIC)
     return fail(c, -1, "unknown kernel variant %d", l->variant);
+  if (c->has_net && is_coop(l->variant)) {
+    if (!coop_supports(c->net))
+      return fail(c, -1, "the cooperative kernels do not support these options (linear update, NEWTON activity "
+                         "algorithm or activity of water)");
+    const int nb = coop_blocks_per_sm(coop_lanes(l->variant), c->net, l->block_threads);
+    if (nb < 1) return fail(c, -1, "cooperative kernel with %d threads per block does not fit on an SM", l->block_threads);
+    if (l->blocks_per_sm > nb) return fail(c, -1, "at most %d blocks of %d threads fit on an SM", nb, l->block_threads);
+    c->launch = *l;
+    c->launch_forced = true;
+    return 0;
+  }
   if (c->has_net) {
     if (is_specialized(l->variant) && !specialized_supports(c->net))
       return fail(c, -1, "the network-specialized kernel does not support the NEWTON activity algorithm at every "
@@ -975,6 +1010,27 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
       }
     }
     if (rc < 0) break;
+  }
+  // cooperative kernels: 8, 16 or 32 lanes per cell, 128-thread blocks
+  if (rc >= 0 && coop_supports(n)) {
+    for (int variant : {PFCHEM_KERNEL_COOP8, PFCHEM_KERNEL_COOP16, PFCHEM_KERNEL_COOP32}) {
+      const int nb = coop_blocks_per_sm(coop_lanes(variant), n, 128);
+      for (int bps = nb; bps >= std::max(1, nb - 1) && nb >= 1 && rc >= 0; --bps) {
+        pfchem_launch l{128, bps, 1, variant};
+        c->launch = l;
+        double ms = 1e30;
+        for (int rep = 0; rep < 2; ++rep) {
+          rc = pfchem_react_batch(c, dt, cl);
+          if (rc < 0) break;
+          ms = std::min(ms, c->stats.kernel_ms);
+          for (auto &x : arrs) cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);
+        }
+        if (rc >= 0 && ms < best) {
+          best = ms;
+          best_l = l;
+        }
+      }
+    }
   }
   for (auto &x : arrs) {
     cudaMemcpyAsync(x.p, x.save, x.bytes, cudaMemcpyDeviceToDevice, c->stream);

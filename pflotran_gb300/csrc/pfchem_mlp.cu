@@ -613,6 +613,8 @@ Surrogate *surrogate_create(int N, uint64_t seed, std::string *err) {
   if (e == cudaSuccess) e = cudaMalloc(&s->m2, off * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->wb, off * sizeof(bf16));
   if (e == cudaSuccess) e = cudaMalloc(&s->wpk, off * sizeof(bf16));
+  // split-K partials: the largest weight block is kHidden x kHidden
+  if (e == cudaSuccess) e = cudaMalloc(&s->ws, (size_t)kSplits * kHidden * kHidden * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->fmu, 2 * kFeat * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->tmu, 2 * kOut * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->loss, sizeof(float));
@@ -645,6 +647,7 @@ void surrogate_destroy(Surrogate *s) {
   cudaFree(s->m2);
   cudaFree(s->wb);
   cudaFree(s->wpk);
+  cudaFree(s->ws);
   cudaFree(s->fmu);
   cudaFree(s->tmu);
   cudaFree(s->loss);
