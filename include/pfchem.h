@@ -368,9 +368,15 @@ int pfchem_equilibrate_constraints(pfchem_ctx *ctx, pfchem_cells *cells, const p
  *   area_m   = area0_m * (porosity/porosity0)^p_por,m * (phi_m/phi0_m)^p_vf,m
  * with the porosity factor only when surface_area_with_porosity and the
  * volume-fraction factor only where phi0_m > 0.  All cells, active or not,
- * as the reference.  The mineral-armoring branch (:1737-1765) is not
- * supported: it carries a flag from cell to cell, so its result depends on
- * the cell order.  Device pointers. */
+ * as the reference.  Mineral armoring (:1737-1765): a mineral with a
+ * critical volume fraction loses its area (0) where its armoring mineral's
+ * volume fraction reaches it; below it the area is scaled by
+ * ((crit - phi_armor)/crit)^p_vf,m, or reset to area0_m right after an
+ * armored item.  The reference carries that "just armored" flag from item to
+ * item in cell-then-mineral order; each armored item sets it from its own
+ * test, so an item's incoming flag is the test of the previous armored item
+ * (the previous cell's last one for a cell's first), and the update stays
+ * data-parallel with the same result.  Device pointers, except armor_flag_out. */
 typedef struct pfchem_mineral_update {
   int32_t update_porosity;             /* reaction%update_porosity                       */
   int32_t update_surface_area;         /* reaction%update_mineral_surface_area           */
@@ -383,6 +389,14 @@ typedef struct pfchem_mineral_update {
   const double *mnrl_area0;            /* (nkinmnrl, ncells) rt_auxvar%mnrl_area0        */
   const double *porosity0;             /* (ncells) field%porosity0, or NULL without the porosity factor */
   double *porosity;                    /* (ncells) out: porosity_base when update_porosity, else NULL */
+  /* mineral armoring (realization_subsurface.F90:1737-1765), with
+   * reaction%update_armor_mineral_surface; NULL tables = off */
+  const double *armor_crit_vol_frac;   /* (nkinmnrl) kinmnrl_armor_crit_vol_frac; <= 0: not armored */
+  const int32_t *armor_mineral;        /* (nkinmnrl) 1-based mineral whose volume fraction armors it
+                                          (kinmnrl_armor_min_names matched to kinmnrl_names; itself if none) */
+  int32_t armor_flag;                  /* in: reaction%update_armor_mineral_surface_flag before the call */
+  int32_t reserved2;
+  int32_t *armor_flag_out;             /* host, out: the flag after the last cell, or NULL */
 } pfchem_mineral_update;
 /* Reads cells->mnrl_volfrac (and cells->porosity when porosity is not
  * updated), writes cells->mnrl_area and mu->porosity. */

@@ -1324,6 +1324,7 @@ int pfo_reaction_blocks(const pfchem_network *net, const pfchem_options *opt, pf
 int pfo_update_mineral_properties(const pfchem_network *net, pfchem_cells *cells, const pfchem_mineral_update *mu) {
   const int Nm = net->nkinmnrl;
   const int64_t n = cells->ncells;
+  int armor_flag = mu->armor_flag;  // reaction%update_armor_mineral_surface_flag
   for (int64_t k = 0; k < n; ++k) {
     double por = cells->porosity[k];
     if (mu->update_porosity && Nm > 0) {
@@ -1342,8 +1343,28 @@ int pfo_update_mineral_properties(const pfchem_network *net, pfchem_cells *cells
         volfrac_scale = std::pow(cells->mnrl_volfrac[m * n + k] / mu->mnrl_volfrac0[m * n + k],
                                  mu->surf_area_vol_frac_pwr[m]);
       cells->mnrl_area[m * n + k] = mu->mnrl_area0[m * n + k] * porosity_scale * volfrac_scale;
+      // realization_subsurface.F90:1737-1765 mineral armoring, with the flag
+      // carried from item to item in loop order
+      if (mu->armor_crit_vol_frac && mu->armor_crit_vol_frac[m] > 0.0) {
+        const int ma = mu->armor_mineral ? mu->armor_mineral[m] - 1 : m;
+        const double crit = mu->armor_crit_vol_frac[m];
+        const double vfa = cells->mnrl_volfrac[ma * n + k];
+        if (crit > vfa) {
+          if (armor_flag == 0)
+            cells->mnrl_area[m * n + k] =
+                cells->mnrl_area[m * n + k] * std::pow((crit - vfa) / crit, mu->surf_area_vol_frac_pwr[m]);
+          else {
+            cells->mnrl_area[m * n + k] = mu->mnrl_area0[m * n + k];
+            armor_flag = 0;
+          }
+        } else {
+          cells->mnrl_area[m * n + k] = 0.0;
+          armor_flag = 1;
+        }
+      }
     }
   }
+  if (mu->armor_flag_out) *mu->armor_flag_out = armor_flag;
   return 0;
 }
 

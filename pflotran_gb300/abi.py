@@ -146,13 +146,16 @@ class MineralUpdate(C.Structure):
                 ("surface_area_with_porosity", C.c_int32), ("reserved", C.c_int32),
                 ("minimum_porosity", C.c_double), ("surf_area_vol_frac_pwr", C.c_void_p),
                 ("surf_area_porosity_pwr", C.c_void_p), ("mnrl_volfrac0", C.c_void_p), ("mnrl_area0", C.c_void_p),
-                ("porosity0", C.c_void_p), ("porosity", C.c_void_p)]
+                ("porosity0", C.c_void_p), ("porosity", C.c_void_p),
+                ("armor_crit_vol_frac", C.c_void_p), ("armor_mineral", C.c_void_p), ("armor_flag", C.c_int32),
+                ("reserved2", C.c_int32), ("armor_flag_out", C.c_void_p)]
 
 
 def mineral_update(arrays, update_porosity=1, update_surface_area=1, surface_area_with_porosity=0,
-                   minimum_porosity=0.0):
+                   minimum_porosity=0.0, armor_flag=0):
     """MineralUpdate over `arrays` (dict of numpy arrays or torch tensors keyed
-    by the pointer fields); the arrays must stay alive while it is used."""
+    by the pointer fields, armor_flag_out a host int32 numpy array); the
+    arrays must stay alive while it is used."""
     def ptr(k):
         a = arrays.get(k)
         if a is None:
@@ -160,7 +163,8 @@ def mineral_update(arrays, update_porosity=1, update_surface_area=1, surface_are
         return a.data_ptr() if hasattr(a, "data_ptr") else a.ctypes.data
     return MineralUpdate(update_porosity, update_surface_area, surface_area_with_porosity, 0, minimum_porosity,
                          ptr("surf_area_vol_frac_pwr"), ptr("surf_area_porosity_pwr"), ptr("mnrl_volfrac0"),
-                         ptr("mnrl_area0"), ptr("porosity0"), ptr("porosity"))
+                         ptr("mnrl_area0"), ptr("porosity0"), ptr("porosity"), ptr("armor_crit_vol_frac"),
+                         ptr("armor_mineral"), int(armor_flag), 0, ptr("armor_flag_out"))
 
 CONSTRAINT_TOTAL, CONSTRAINT_FREE, CONSTRAINT_CHARGE_BAL, CONSTRAINT_PH, CONSTRAINT_LOG, CONSTRAINT_MINERAL = 1, 2, 3, 4, 5, 6
 

@@ -26,7 +26,8 @@ cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int g
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
 cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const int32_t *type, const int32_t *mineral,
                               const double *value, int max_its, Scratch *scr, cudaStream_t st);
-cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, cudaStream_t st);
+cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, int *flag_dev,
+                                      cudaStream_t st);
 cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
                                    double *dtotal, double *total_sorb, double *dtotal_sorb, cudaStream_t st);
 int max_active_blocks(const DevNet &n, int block);
@@ -865,12 +866,23 @@ int pfchem_update_mineral_properties(pfchem_ctx *c, pfchem_cells *cl, const pfch
     if (mu->surface_area_with_porosity && (!mu->surf_area_porosity_pwr || !mu->porosity0))
       return fail(c, -1, "surf_area_porosity_pwr and porosity0 required with surface_area_with_porosity");
   }
+  if (mu->armor_crit_vol_frac && mu->update_surface_area && Nm > 0 && !mu->surf_area_vol_frac_pwr)
+    return fail(c, -1, "armoring needs surf_area_vol_frac_pwr");
   cudaSetDevice(c->device);
   CellArgs a = device_args(cl, 1.0);
-  if (a.ncells == 0) return 0;
-  cudaError_t le = launch_mineral_properties(a, Nm, *mu, c->stream);
+  if (a.ncells == 0) {
+    if (mu->armor_flag_out) *mu->armor_flag_out = mu->armor_flag;
+    return 0;
+  }
+  // the flag after the last cell comes back through the context's scratch
+  int *flag_dev = reinterpret_cast<int *>(&c->scratch->armor_flag);
+  cudaError_t le = launch_mineral_properties(a, Nm, *mu, flag_dev, c->stream);
   if (le != cudaSuccess) return fail(c, -2, "mineral-properties launch: %s", cudaGetErrorString(le));
+  int flag = mu->armor_flag;
+  if (mu->armor_flag_out && mu->update_surface_area)
+    CUDA_TRY(c, cudaMemcpyAsync(&flag, flag_dev, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  if (mu->armor_flag_out) *mu->armor_flag_out = flag;
   return 0;
 }
 

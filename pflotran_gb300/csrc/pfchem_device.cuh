@@ -103,7 +103,9 @@ struct DevNet {
   unsigned long long t_drain_inv;  /* ~(first time the queue ran dry), ns */ \
   unsigned long long t_end;        /* last warp exit, ns */ \
   unsigned int max_iter;                              \
-  unsigned int nonconverged;
+  unsigned int nonconverged;                          \
+  unsigned int armor_flag; /* mineral armoring flag after the last cell */ \
+  unsigned int pad_;
 
 struct CellArgs {
   PFCHEM_CELLARGS_FIELDS

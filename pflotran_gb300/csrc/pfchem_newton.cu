@@ -1303,7 +1303,7 @@ static cudaError_t launch_constraint_t(const DevNet &n, const CellArgs &a, const
 
 // Mineral-driven porosity and surface area (one thread per cell).
 __global__ void __launch_bounds__(128) mineral_properties_kernel(const __grid_constant__ CellArgs a, int Nm,
-                                                                 pfchem_mineral_update mu) {
+                                                                 pfchem_mineral_update mu, int *flag_dev) {
   const int64_t cell = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   const int64_t nc = a.ncells;
   if (cell >= nc) return;
@@ -1316,20 +1316,48 @@ __global__ void __launch_bounds__(128) mineral_properties_kernel(const __grid_co
   }
   if (!mu.update_surface_area) return;
   const double ratio = mu.surface_area_with_porosity ? por / mu.porosity0[cell] : 1.0;
+  // armoring: the reference's flag entering this cell is set by the test of
+  // the previous cell's last armored mineral (the caller's flag for cell 0)
+  int flag = mu.armor_flag;
+  int last = -1;
+  if (mu.armor_crit_vol_frac) {
+    for (int k = 0; k < Nm; ++k)
+      if (mu.armor_crit_vol_frac[k] > 0.0) last = k;
+    if (last >= 0 && cell > 0) {
+      const int ma = mu.armor_mineral ? mu.armor_mineral[last] - 1 : last;
+      flag = mu.armor_crit_vol_frac[last] > a.vf[ma * nc + cell - 1] ? 0 : 1;
+    }
+  }
   for (int k = 0; k < Nm; ++k) {
     double ps = 1.0;
     if (mu.surface_area_with_porosity) ps = pow(ratio, mu.surf_area_porosity_pwr[k]);
     double vs = 1.0;
     const double vf0 = mu.mnrl_volfrac0[k * nc + cell];
     if (vf0 > 0.0) vs = pow(a.vf[k * nc + cell] / vf0, mu.surf_area_vol_frac_pwr[k]);
-    a.area[k * nc + cell] = mu.mnrl_area0[k * nc + cell] * ps * vs;
+    double area = mu.mnrl_area0[k * nc + cell] * ps * vs;
+    if (mu.armor_crit_vol_frac && mu.armor_crit_vol_frac[k] > 0.0) {
+      const int ma = mu.armor_mineral ? mu.armor_mineral[k] - 1 : k;
+      const double crit = mu.armor_crit_vol_frac[k];
+      const double vfa = a.vf[ma * nc + cell];
+      if (crit > vfa) {
+        area = flag == 0 ? area * pow((crit - vfa) / crit, mu.surf_area_vol_frac_pwr[k]) : mu.mnrl_area0[k * nc + cell];
+        flag = 0;
+      } else {
+        area = 0.0;
+        flag = 1;
+      }
+    }
+    a.area[k * nc + cell] = area;
   }
+  // the flag after the last cell (the caller's flag if nothing is armored)
+  if (cell == nc - 1 && flag_dev) *flag_dev = flag;
 }
 
-cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, cudaStream_t st) {
+cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, int *flag_dev,
+                                      cudaStream_t st) {
   const int block = 128;
   const int64_t grid = (a.ncells + block - 1) / block;
-  mineral_properties_kernel<<<(unsigned)grid, block, 0, st>>>(a, Nm, mu);
+  mineral_properties_kernel<<<(unsigned)grid, block, 0, st>>>(a, Nm, mu, flag_dev);
   return cudaGetLastError();
 }
 

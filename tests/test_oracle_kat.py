@@ -188,3 +188,45 @@ def test_single_cell_constraint_rejects_rows_it_cannot_take(oracle):
     for bad in ([1, 1, 6], [1, 0, 1], [7, 1, 1]):
         with pytest.raises(RuntimeError):
             oracle.equilibrate_constraint(net.as_struct(), default_options(use_isothermal=1), b, bad, [1e-5] * 3)
+
+
+def test_armoring_flag_is_set_by_the_previous_armored_item(oracle):
+    """The reference carries the armoring flag from item to item (cells, then
+    minerals); every armored item sets it from its own test, so the serial
+    loop equals the data-parallel rule the GPU kernel uses: an item's incoming
+    flag is the test of the previous armored item.  Checked on the oracle's
+    serial restatement against that rule written out here."""
+    from pflotran_gb300 import abi, workloads
+    net, opt, cells, dt = workloads.synthetic_cells(257, seed=36)
+    n, Nm = cells.ncells, net.Nm
+    rng = np.random.default_rng(5)
+    vf = rng.uniform(0.0, 0.05, (Nm, n))
+    cells.mnrl_volfrac = vf.ravel().copy()
+    crit = np.zeros(Nm)
+    crit[1], crit[3], crit[4] = 0.025, 0.03, 0.01
+    armor = np.arange(1, Nm + 1, dtype=np.int32)
+    armor[1], armor[3] = 1, 6
+    area0 = rng.uniform(0.5, 2.0, (Nm, n))
+    vf0 = rng.uniform(0.01, 0.05, (Nm, n))
+    pw = np.full(Nm, 2.0 / 3.0)
+    for flag_in in (0, 1):
+        out = np.full(1, -1, np.int32)
+        c = cells.copy()
+        oracle.update_mineral_properties(net.as_struct(), c, abi.mineral_update(
+            {"surf_area_vol_frac_pwr": pw, "mnrl_volfrac0": vf0.ravel(), "mnrl_area0": area0.ravel(),
+             "armor_crit_vol_frac": crit, "armor_mineral": armor, "armor_flag_out": out},
+            update_porosity=0, armor_flag=flag_in))
+        expect = area0 * (vf / vf0) ** pw[:, None]
+        items = [m for m in range(Nm) if crit[m] > 0]
+        test = lambda m, k: crit[m] > vf[armor[m] - 1, k]
+        for k in range(n):
+            for i, m in enumerate(items):
+                prev = (items[i - 1], k) if i > 0 else ((items[-1], k - 1) if k > 0 else None)
+                flag = flag_in if prev is None else (0 if test(*prev) else 1)
+                if test(m, k):
+                    fa = ((crit[m] - vf[armor[m] - 1, k]) / crit[m]) ** pw[m]
+                    expect[m, k] = expect[m, k] * fa if flag == 0 else area0[m, k]
+                else:
+                    expect[m, k] = 0.0
+        np.testing.assert_allclose(c.mnrl_area.reshape(Nm, n), expect, rtol=1e-14, atol=0)
+        assert out[0] == (0 if test(items[-1], n - 1) else 1)

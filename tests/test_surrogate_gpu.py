@@ -48,7 +48,8 @@ def test_gradients_match_fp64_oracle():
                 continue
             rel = np.linalg.norm(a - b) / np.linalg.norm(b)
             print(f"layer {l} {'weights' if size == k * n else 'bias'}: relative L2 error {rel:.3e}")
-            assert rel < 2e-2, (l, size, rel)
+            # measured on GB300: at most 1.5e-4 (layer 0 weights); bar 2e-3
+            assert rel < 2e-3, (l, size, rel)
 
 
 def test_fused_inference_equals_layer_by_layer():
