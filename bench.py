@@ -79,6 +79,8 @@ def parse():
                    help="also time the plain step with exact_jacobian_after = 0")
     p.add_argument("--calcite-grid", action=argparse.BooleanOptionalAction, default=True)
     p.add_argument("--timestepped", action=argparse.BooleanOptionalAction, default=True)
+    p.add_argument("--mapping", action=argparse.BooleanOptionalAction, default=True,
+                   help="thread-per-cell vs cooperative kernels on three network sizes")
     p.add_argument("--jacobian", choices=("reference", "exact"), default="reference",
                    help="Newton Jacobian of the headline run")
     return p.parse_args()
@@ -295,6 +297,64 @@ def calcite_grid(args, local):
             "ms_per_step": float(np.mean(ms)), "mean_newton_iterations": float(np.mean(its)),
             "nonconverged": int(host.ncells - conv[-1]),
             "parity": {"cells": int(both.sum()), **parity.error_statement(net, gsub, ref, both)}}
+
+
+def mapping_by_size(args, local, ncells=262144):
+    """Thread-per-cell (network-specialized) against cooperative kernels
+    (8/16/32 lanes per cell) by network size: device time of one step
+    (best of 2 after a warm-up) on `ncells` cells of three networks, and the
+    launch pfchem_autotune keeps for each."""
+    from pflotran_gb300 import abi, workloads
+    from pflotran_gb300.lib import PfchemError, ReactionStep
+    nets = {"calcite (N=3, 5 complexes, 1 mineral)":
+            workloads.calcite_cells(ncells, seed=3, temperature_dependent=True, device=f"cuda:{local}"),
+            "synthetic (N=12, 40 complexes, 6 minerals, 4 exchange, 2 surface)":
+            workloads.synthetic_cells(ncells, seed=5, device=f"cuda:{local}"),
+            "synthetic (N=16, 64 complexes, 8 minerals, 4 exchange, 2 surface)":
+            workloads.synthetic_cells(ncells, seed=5, net=workloads.synthetic_network(N=16, Nc=64, Nm=8),
+                                      device=f"cuda:{local}")}
+    names = {abi.KERNEL_SPECIALIZED: "thread-per-cell specialized", abi.KERNEL_SPECIALIZED_COMPACT:
+             "thread-per-cell specialized, compact", abi.KERNEL_COOP8: "8 lanes per cell",
+             abi.KERNEL_COOP16: "16 lanes per cell", abi.KERNEL_COOP32: "32 lanes per cell (warp)"}
+    out = {}
+    for label, (net, opt, host, dt) in nets.items():
+        step = ReactionStep(net, opt, device=local)
+        pristine = host.to_device()
+        res = {}
+        default = step.launch()
+        for variant in names:
+            block = 32 if variant in (abi.KERNEL_SPECIALIZED, abi.KERNEL_SPECIALIZED_COMPACT) else 128
+            try:
+                bps = None
+                for b in range(16, 0, -1):  # as many resident blocks per SM as fit
+                    try:
+                        step.set_launch(block, b, 1, variant)
+                        bps = b
+                        break
+                    except PfchemError:
+                        continue
+                if bps is None:
+                    raise PfchemError("does not fit on an SM")
+                times, its, bad = [], 0.0, 0
+                for rep in range(3):
+                    dev = pristine.copy()
+                    step.react(dev, dt)
+                    st = step.stats()
+                    if rep:
+                        times.append(st.kernel_ms)
+                    its, bad = st.sum_iterations / st.ncells, int(st.nonconverged)
+                res[names[variant]] = {"ms": min(times), "block_threads": block, "blocks_per_sm": bps,
+                                       "mean_newton_iterations": its, "nonconverged": bad}
+            except Exception as e:  # a mapping that does not apply to this network
+                res[names[variant]] = {"error": str(e)[:200]}
+        tuned = step.autotune(pristine.copy(), dt)
+        res["autotune_choice"] = {"variant": names.get(tuned.variant, tuned.variant),
+                                  "block_threads": tuned.block_threads, "blocks_per_sm": tuned.blocks_per_sm,
+                                  "refill_min_idle": tuned.refill_min_idle}
+        res["library_default"] = names.get(default.variant, default.variant)
+        out[label] = res
+        del step, pristine
+    return {"cells": ncells, "networks": out}
 
 
 def timestepped(args, local):
@@ -643,6 +703,8 @@ def main():
         line["calcite_grid"] = calcite_grid(args, local)
     if rank == 0 and args.timestepped:
         line["timestepped"] = timestepped(args, local)
+    if rank == 0 and args.mapping:
+        line["mapping_by_size"] = mapping_by_size(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

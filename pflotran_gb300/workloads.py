@@ -70,10 +70,11 @@ def calcite_network(temperature_dependent=False, seed=0, delta=0.3):
 
 
 def synthetic_network(seed=3, N=12, Nc=40, Nm=6, Nix=4, Nsr=2, porosity=0.25, rho_s=2650.0):
-    """Seeded synthetic network with the sizes of the 12-species workload."""
+    """Seeded synthetic network with the sizes of the 12-species workload
+    (other sizes up to 16 primaries for the kernel-mapping comparison)."""
     rng = np.random.default_rng(seed)
     # charges: >= 4 cations (Z > 0) for ion exchange, the rest in {-2..2}
-    Z = np.array([1, 2, 1, 2, 1, -1, -2, -1, 0, 1, -1, 2], dtype=float)[:N]
+    Z = np.array([1, 2, 1, 2, 1, -1, -2, -1, 0, 1, -1, 2, 1, -1, 0, 2], dtype=float)[:N]
     rng.shuffle(Z)
     # species 0 plays the part of H+: the only species with negative
     # coefficients (deprotonation reactions), so only its total can be < 0
