@@ -46,6 +46,8 @@ KERNEL_COOP16 = 4
 KERNEL_COOP32 = 5
 JACOBIAN_REFERENCE = 0
 JACOBIAN_EXACT = 1
+MLP_MMA_SYNC = 0
+MLP_TCGEN05 = 1
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)

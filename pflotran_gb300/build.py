@@ -17,7 +17,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libpfchem.so")
 PROBE = os.path.join(OUT, "libpfchem_probe.so")
 SOURCES = ["pfchem_newton.cu", "pfchem_api.cu", "pfchem_noalloc.cu", "pfchem_codegen.cu", "pfchem_mlp.cu",
-           "pfchem_coop.cu"]
+           "pfchem_coop.cu", "pfchem_umma.cu"]
 PROBE_SOURCES = ["fp64_peak.cu"]
 TRANSPORT = os.path.join(OUT, "libpfchem_transport.so")
 TRANSPORT_SOURCES = ["transport_upwind.cu"]

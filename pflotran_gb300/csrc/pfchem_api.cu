@@ -70,6 +70,8 @@ cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, fl
 void surrogate_mark_trained(Surrogate *s, bool t);
 bool surrogate_trained(const Surrogate *s);
 bool surrogate_ready(const Surrogate *s, long long ncells);
+void surrogate_set_backend(Surrogate *s, int backend);
+cudaError_t surrogate_check(Surrogate *s, bool *timed_out);
 }  // namespace pfchem
 
 using namespace pfchem;
@@ -1176,6 +1178,11 @@ int pfchem_surrogate_fit(pfchem_ctx *c, const float *X, const double *molal, int
   cudaEventDestroy(t1);
   cudaFree(T);
   if (ce != cudaSuccess) return fail(c, -2, "training: %s", cudaGetErrorString(ce));
+  {
+    bool to = false;
+    CUDA_TRY(c, surrogate_check(c->sur, &to));
+    if (to) return fail(c, -2, "training: a tensor-core kernel's wait ran out");
+  }
   surrogate_mark_trained(c->sur, true);
   if (c->graph) {
     cudaGraphExecDestroy(c->graph);
@@ -1204,6 +1211,23 @@ int pfchem_surrogate_predict(pfchem_ctx *c, pfchem_cells *cl, double *guess) {
   CUDA_TRY(c, cudaMemcpyAsync(guess, surrogate_guess_buffer(c->sur), (size_t)c->net.N * a.ncells * sizeof(double),
                               cudaMemcpyDeviceToDevice, c->stream));
   CUDA_TRY(c, cudaStreamSynchronize(c->stream));
+  bool to = false;
+  CUDA_TRY(c, surrogate_check(c->sur, &to));
+  if (to) return fail(c, -2, "prediction: a tensor-core kernel's wait ran out");
+  return 0;
+}
+
+int pfchem_surrogate_backend(pfchem_ctx *c, int backend) {
+  if (!c) return -1;
+  if (backend != PFCHEM_MLP_MMA_SYNC && backend != PFCHEM_MLP_TCGEN05) return fail(c, -1, "unknown backend %d", backend);
+  cudaSetDevice(c->device);
+  int e = need_surrogate(c, 1);
+  if (e) return e;
+  surrogate_set_backend(c->sur, backend);
+  if (c->graph) {
+    cudaGraphExecDestroy(c->graph);
+    c->graph = nullptr;
+  }
   return 0;
 }
 

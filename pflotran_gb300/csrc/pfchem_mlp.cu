@@ -31,6 +31,12 @@
 
 namespace pfchem {
 
+cudaError_t umma_prepare();
+bool umma_supports(int N, int K, bool w_kn);
+cudaError_t umma_linear(cudaStream_t st, const __nv_bfloat16 *X, long long rows, int K, const __nv_bfloat16 *W, int N,
+                        bool w_kn, const float *bias, float *Cf, __nv_bfloat16 *Cb, int epi, int *err, int sms);
+constexpr int kUmmaGeluE = 0, kUmmaLinearE = 1;  // umma_linear epilogues
+
 constexpr int kFeat = 16;    // input features
 constexpr int kHidden = 256;  // hidden width
 constexpr int kOut = PFCHEM_MAX_PRI;  // outputs (the first N used)
@@ -505,6 +511,11 @@ struct Surrogate {
   int steps = 0;
   uint32_t *wpk = nullptr;  // B-fragment packing of the BF16 weights (fused inference)
   float *ws = nullptr;      // split-K partials of the weight gradients (kSplits x 256 x 256)
+  // tensor-core path of the dense layers: 0 = mma.sync (warp-level MMA, the
+  // fused one-kernel inference), 1 = tcgen05.mma with tensor-memory accumulators
+  int backend = 0;
+  int *uerr = nullptr;      // set by a tcgen05 kernel whose wait ran out
+  int sms = 0;
 };
 constexpr int kSplits = 16;  // weight-gradient GEMMs: K = batch rows split 16 ways
 
@@ -552,10 +563,16 @@ void forward(Surrogate *s, long long rows, cudaStream_t st, bool keep) {
     const int K = s->dims[l], Nn = s->dims[l + 1];
     const bf16 *W = s->wb + s->woff[l];
     const float *b = s->w + s->boff[l];
-    if (l < kLayers - 1)
+    if (s->backend == 1 && umma_supports(Nn, K, true)) {
+      if (l < kLayers - 1)
+        umma_linear(st, in, rows, K, W, Nn, true, b, keep ? s->z[l] : nullptr, s->hb[l], kUmmaGeluE, s->uerr, s->sms);
+      else
+        umma_linear(st, in, rows, K, W, Nn, true, b, s->y, nullptr, kUmmaLinearE, s->uerr, s->sms);
+    } else if (l < kLayers - 1) {
       gemm<kEpiAct>(st, in, K, 1, W, Nn, 1, (int)rows, Nn, K, b, keep ? s->z[l] : nullptr, s->hb[l], Nn, 1);
-    else
+    } else {
       gemm<kEpiF32>(st, in, K, 1, W, Nn, 1, (int)rows, Nn, K, b, s->y, nullptr, Nn, 0);
+    }
     in = s->hb[l];
   }
 }
@@ -579,7 +596,10 @@ void backward(Surrogate *s, long long rows, cudaStream_t st) {
     if (l > 0) {
       // dH_{l-1} [rows x K] = dZ [rows x N] . W^T, W stored [K x N]
       const bf16 *W = s->wb + s->woff[l];
-      gemm<kEpiF32>(st, dZb, Nn, 1, W, 1, Nn, (int)rows, K, Nn, nullptr, s->dz[l - 1], nullptr, K, 0);
+      if (s->backend == 1 && umma_supports(K, Nn, false))
+        umma_linear(st, dZb, rows, Nn, W, K, false, nullptr, s->dz[l - 1], nullptr, kUmmaLinearE, s->uerr, s->sms);
+      else
+        gemm<kEpiF32>(st, dZb, Nn, 1, W, 1, Nn, (int)rows, K, Nn, nullptr, s->dz[l - 1], nullptr, K, 0);
       // through the GELU of layer l-1: dZ_{l-1} = dH * GELU'(Z_{l-1}) (in place in dz)
       gelu_backward<<<blocks(rows * K, 256), 256, 0, st>>>(s->dz[l - 1], s->z[l - 1], s->db[l - 1], s->dz[l - 1],
                                                            rows * K);
@@ -618,9 +638,17 @@ Surrogate *surrogate_create(int N, uint64_t seed, std::string *err) {
   if (e == cudaSuccess) e = cudaMalloc(&s->fmu, 2 * kFeat * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->tmu, 2 * kOut * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->loss, sizeof(float));
+  if (e == cudaSuccess) e = cudaMalloc(&s->uerr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(s->uerr, 0, sizeof(int));
+  if (e == cudaSuccess) e = umma_prepare();
   if (e != cudaSuccess) {
     *err = cudaGetErrorString(e);
     return nullptr;
+  }
+  {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, dev);
   }
   s->fsd = s->fmu + kFeat;
   s->tsd = s->tmu + kOut;
@@ -648,6 +676,7 @@ void surrogate_destroy(Surrogate *s) {
   cudaFree(s->wb);
   cudaFree(s->wpk);
   cudaFree(s->ws);
+  cudaFree(s->uerr);
   cudaFree(s->fmu);
   cudaFree(s->tmu);
   cudaFree(s->loss);
@@ -770,9 +799,14 @@ cudaError_t surrogate_pack(Surrogate *s, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+cudaError_t surrogate_predict_layers(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess,
+                                     cudaStream_t st);
+
 cudaError_t surrogate_predict(Surrogate *s, const DevNet &n, const CellArgs &a, double *guess, cudaStream_t st,
                               bool pack) {
   const long long nc = a.ncells;
+  // tcgen05 backend: layer by layer, each layer's weights resident in shared memory
+  if (s->backend == 1) return surrogate_predict_layers(s, n, a, guess, st);
   if (pack) {
     cudaError_t e = surrogate_pack(s, st);
     if (e != cudaSuccess) return e;
@@ -821,6 +855,16 @@ cudaError_t surrogate_targets(Surrogate *s, const double *molal, long long M, fl
 int surrogate_nfeat() { return kFeat; }
 void surrogate_mark_trained(Surrogate *s, bool t) { s->trained = t; }
 bool surrogate_trained(const Surrogate *s) { return s->trained; }
+void surrogate_set_backend(Surrogate *s, int backend) { s->backend = backend; }
+int surrogate_backend(const Surrogate *s) { return s->backend; }
+// Reads and clears the tcgen05 kernels' timeout flag.
+cudaError_t surrogate_check(Surrogate *s, bool *timed_out) {
+  int h = 0;
+  cudaError_t e = cudaMemcpy(&h, s->uerr, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && h) e = cudaMemset(s->uerr, 0, sizeof(int));
+  *timed_out = h != 0;
+  return e;
+}
 // True when surrogate_predict can run on `ncells` cells without allocating.
 bool surrogate_ready(const Surrogate *s, long long ncells) {
   return s->cap >= std::min(ncells, kChunk) && s->feat_cap >= ncells && s->guess_cap >= ncells;

@@ -98,6 +98,7 @@ def _surrogate_bind(l):
     l.pfchem_surrogate_params.argtypes = [vp, vp, C.c_int]
     l.pfchem_surrogate_params.restype = C.c_int64
     l.pfchem_surrogate_normalization.argtypes = [vp, vp, vp, vp, vp, C.c_int]
+    l.pfchem_surrogate_backend.argtypes = [vp, C.c_int]
 
 
 class WarmStartMixin:
@@ -140,6 +141,11 @@ class WarmStartMixin:
         self._check(self._lib.pfchem_surrogate_predict_layers(self._ctx, C.byref(s), C.c_void_p(g.data_ptr())),
                     "pfchem_surrogate_predict_layers")
         return g
+
+    def surrogate_backend(self, backend):
+        """Tensor-core path of the dense layers: abi.MLP_MMA_SYNC or abi.MLP_TCGEN05."""
+        _surrogate_bind(self._lib)
+        self._check(self._lib.pfchem_surrogate_backend(self._ctx, int(backend)), "pfchem_surrogate_backend")
 
     def surrogate_enable(self, on=True):
         _surrogate_bind(self._lib)

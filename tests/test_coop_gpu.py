@@ -40,7 +40,10 @@ def _solve(step, variant, cells, dt):
 
 def _check(net, opt, dt, cells, gpu, ref):
     ok = (ref.status == 0) & (gpu.status == 0)
-    assert ok.mean() > 0.999, (np.bincount(ref.status), np.bincount(gpu.status))
+    # the GPU reports the oracle's per-cell status (some draws have cells
+    # whose inner loops hit their caps in both)
+    assert np.mean(ref.status == gpu.status) > 0.999, (np.bincount(ref.status), np.bincount(gpu.status))
+    assert ok.mean() > 0.99
     same = ok & (ref.iterations == gpu.iterations)
     assert same.sum() > 0.98 * ok.sum()
     gpu.sec_molal = None
