@@ -494,7 +494,25 @@ def main():
         inference = {"ms": min(inf_ms), "tflops": inf_flops / (min(inf_ms) * 1e-3) / 1e12,
                      "flops": inf_flops,
                      "frac_of_bf16_peak": inf_flops / (min(inf_ms) * 1e-3) / 1e12 / _bf16_peak(),
-                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"}
+                     "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)",
+                     "backend": "mma.sync fused one-kernel inference"}
+        # the same inference on the tcgen05 path (layer by layer, TMEM accumulators)
+        from pflotran_gb300 import abi as _abi
+        try:
+            step.surrogate_backend(_abi.MLP_TCGEN05)
+            t_ms = []
+            for _ in range(3):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                g_ = step.surrogate_predict(dev)
+                t_ms.append((time.perf_counter() - t0) * 1e3)
+                del g_
+            inference["tcgen05"] = {"ms": min(t_ms), "tflops": inf_flops / (min(t_ms) * 1e-3) / 1e12,
+                                    "frac_of_bf16_peak": inf_flops / (min(t_ms) * 1e-3) / 1e12 / _bf16_peak()}
+        except Exception as e:
+            inference["tcgen05"] = {"error": str(e)[:200]}
+        finally:
+            step.surrogate_backend(_abi.MLP_MMA_SYNC)
         step.surrogate_enable(True)
         warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit, inference=inference,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),

@@ -540,7 +540,9 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
           acc(o, "  dsum", n.xzr[r][k], "X" + I(k));
         }
         o << "    if (one_more) break;\n";
-        o << "    const double d = dsum / KD + ref;\n    const double delta = (1.0 - tot) / d;\n";
+        // (1 - tot) / (dsum / KD + ref) with one division: the same Newton
+        // step on KD (reaction.F90:4379-4411), converged to the same 1e-12
+        o << "    const double delta = (1.0 - tot) * KD / fma(ref, KD, dsum);\n";
         o << "    KD = fmax(KD + delta, 1e-40);\n    if (fabs(delta) < 1e-12 * KD) one_more = true;\n  }\n";
         o << "  L.ixr[" << r << "] = X0 * omega * " << lit(1.0 / zref) << ";\n";
       } else {
