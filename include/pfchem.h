@@ -335,9 +335,13 @@ int pfchem_reaction_blocks(pfchem_ctx *ctx, pfchem_cells *cells, pfchem_reaction
  * run, and the learned warm start's training waters.  Types (and mineral
  * ids) are shared by the batch, values are per cell.  Rows: TOTAL [mol/L],
  * FREE [mol/L], LOG (log10 of a free concentration [mol/L]), CHARGE_BAL
- * (value: initial guess [mol/L]), PH (the component is H+; value: pH) and
+ * (value: initial guess [mol/L]), PH (the component is H+; value: pH),
  * MINERAL (the reaction of kinetic mineral mineral[i] held at equilibrium;
- * value: initial guess [mol/L]).  Starts from free ions 1e-9, alternates log
+ * value: initial guess [mol/L]), GAS (reaction.F90:1720-1751: the passive
+ * gas mineral[i] of the gas tables below at partial pressure value [bar]; a
+ * value <= 0 is log10 of the partial pressure, reaction.F90:1531-1535) and
+ * TOTAL_SORB (sorbed total [mol/m^3 bulk], reaction.F90:1608-1614; the
+ * component's equilibrium sorption).  Starts from free ions 1e-9, alternates log
  * and linear updates for iterations 4-8, switches activity coefficients on
  * after the first convergence; converged when max|res| <
  * opt.max_residual_tolerance and the relative change <
@@ -352,12 +356,24 @@ int pfchem_reaction_blocks(pfchem_ctx *ctx, pfchem_cells *cells, pfchem_reaction
 #define PFCHEM_CONSTRAINT_PH 4
 #define PFCHEM_CONSTRAINT_LOG 5
 #define PFCHEM_CONSTRAINT_MINERAL 6
+#define PFCHEM_CONSTRAINT_GAS 7
+#define PFCHEM_CONSTRAINT_TOTAL_SORB 8
+#define PFCHEM_MAX_GAS_ROWS 8    /* GAS rows per constraint */
 typedef struct pfchem_constraint {
   const int32_t *type;     /* (naqcomp) PFCHEM_CONSTRAINT_* (host pointer) */
-  const int32_t *mineral;  /* (naqcomp) 1-based kinetic mineral of MINERAL rows, or NULL (host pointer) */
+  const int32_t *mineral;  /* (naqcomp) constraint_spec_id: 1-based kinetic mineral of MINERAL rows, 1-based
+                              passive gas of GAS rows; or NULL (host pointer) */
   const double *value;     /* (naqcomp, ncells) per-cell values (device pointer) */
   int32_t max_iterations;  /* cap; <= 0 means 10000 */
+  int32_t npassive_gas;    /* gases in the tables below (reaction_gas_aux.F90 gas%paseq*), host pointers */
+  int32_t paseq_ld;        /* leading dimension of paseqspecid (0:paseq_ld) and paseqstoich */
   int32_t reserved;
+  const int32_t *paseqspecid;    /* (0:paseq_ld, npassive_gas): count, then 1-based primary ids */
+  const double *paseqstoich;     /* (paseq_ld, npassive_gas) */
+  const int32_t *paseqh2oid;     /* (npassive_gas) > 0 where H2O takes part, or NULL */
+  const double *paseqh2ostoich;  /* (npassive_gas), or NULL */
+  const double *paseqlogK;       /* (npassive_gas) log10 K (use_isothermal) */
+  const double *paseqlogKcoef;   /* (5, npassive_gas) log K(T) fit (otherwise) */
 } pfchem_constraint;
 int pfchem_equilibrate_constraints(pfchem_ctx *ctx, pfchem_cells *cells, const pfchem_constraint *con);
 

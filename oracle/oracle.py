@@ -140,15 +140,16 @@ def update_mineral_properties(net_struct, cells, mu):
     return lib().pfo_update_mineral_properties(C.byref(net_struct), C.byref(s), C.byref(mu))
 
 
-def equilibrate_constraints(net_struct, opt, cells, types, values, minerals=None, max_iterations=0, nthreads=None):
+def equilibrate_constraints(net_struct, opt, cells, types, values, minerals=None, max_iterations=0, nthreads=None,
+                            gases=None):
     """Restated constraint speciation of every cell of a host CellBatch;
-    `values` (N, ncells).  Returns the number of failed cells."""
+    `values` (N, ncells), `gases` the network's gas_table() for GAS rows.
+    Returns the number of failed cells (< 0: invalid rows)."""
     from pflotran_gb300 import abi
     t = np.ascontiguousarray(types, np.int32)
     mn = None if minerals is None else np.ascontiguousarray(minerals, np.int32)
     v = np.ascontiguousarray(values, np.float64)
-    con = abi.Constraint(t.ctypes.data, None if mn is None else mn.ctypes.data, v.ctypes.data,
-                         int(max_iterations), 0)
+    con = abi.constraint(t, v.ctypes.data, mn, max_iterations, gases)
     s = cells.struct()
     return lib().pfo_equilibrate_constraints(C.byref(net_struct), C.byref(opt), C.byref(s), C.byref(con),
                                              nthreads or os.cpu_count() or 1)

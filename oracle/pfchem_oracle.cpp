@@ -1510,28 +1510,39 @@ double pfo_ifc67_density(double t, double p) {
 
 namespace {
 // Constraint row types of ReactionEquilibrateConstraint (reaction_aux.F90 CONSTRAINT_*)
-enum { kConTotal = 1, kConFree = 2, kConChargeBal = 3, kConPH = 4, kConLog = 5, kConMineral = 6 };
+enum { kConTotal = 1, kConFree = 2, kConChargeBal = 3, kConPH = 4, kConLog = 5, kConMineral = 6, kConGas = 7,
+       kConTotalSorb = 8 };
 
 // reaction.F90:1308-2046 ReactionEquilibrateConstraint with TOTAL [mol/L],
 // FREE [mol/L], LOG (log10 free [mol/L]), CHARGE_BAL, pH (H+ as a primary
-// species) and MINERAL rows (no gas, sorbed-total or colloid rows); a MINERAL
-// row holds the reaction of kinetic mineral `mineral[i]` (1-based) at
-// equilibrium.  Starts from free ions 1e-9 (reaction.F90:1481), alternates
+// species), MINERAL, GAS and TOTAL_SORB rows (no supercritical-CO2 or colloid
+// rows); a MINERAL row holds the reaction of kinetic mineral `mineral[i]`
+// (1-based) at equilibrium, a GAS row the reaction of passive gas
+// `mineral[i]` of `gas`'s tables at partial pressure conc[i] [bar]
+// (reaction.F90:1720-1751), a TOTAL_SORB row the sorbed total conc[i]
+// [mol/m^3 bulk] (:1608-1614).  Starts from free ions 1e-9 (reaction.F90:1481), alternates
 // log/linear updates for iterations 4-8 (:1841-1852) and switches activity
 // coefficients on after the first convergence (:1954-1966).  Returns 0,
 // 1 (iteration cap), 2 (singular), 3 (non-positive molality, :1876-1894).
 template <class R>
 int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, const int *type,
-                           const double *conc, int *iters_out, const int *mineral = nullptr, int max_its = 10000) {
+                           const double *conc_in, int *iters_out, const int *mineral = nullptr, int max_its = 10000,
+                           const pfchem_constraint *gas = nullptr) {
   const int N = w.N;
   const pfchem_network &n = *w.n;
   R convert_molar_to_molal = R(1000) / c.den_kg;
-  R total_conc[P], free_conc[P];
+  R total_conc[P], free_conc[P], gas_logK[P];
+  double conc[P];
   for (int i = 0; i < N; ++i) {
+    conc[i] = conc_in[i];
     free_conc[i] = R(1e-9);
     total_conc[i] = 0;
-    if (type[i] == kConTotal) total_conc[i] = R(conc[i]);
-    else if (type[i] == kConFree || type[i] == kConChargeBal || type[i] == kConMineral)
+    if (type[i] == kConTotal || type[i] == kConTotalSorb) total_conc[i] = R(conc[i]);
+    else if (type[i] == kConGas) {
+      if (conc[i] <= 0.0) conc[i] = std::pow(10.0, conc[i]);  // log10 partial pressure (:1531-1535)
+      const int g = mineral[i] - 1;
+      gas_logK[i] = o.use_isothermal ? R(gas->paseqlogK[g]) : interpolate_logK(gas->paseqlogKcoef + 5 * g, c.temp);
+    } else if (type[i] == kConFree || type[i] == kConChargeBal || type[i] == kConMineral)
       free_conc[i] = R(conc[i]) * convert_molar_to_molal;
     else if (type[i] == kConLog) free_conc[i] = std::pow(R(10), R(conc[i])) * convert_molar_to_molal;
     else if (type[i] == kConPH) free_conc[i] = std::pow(R(10), -R(conc[i]));
@@ -1577,6 +1588,23 @@ int equilibrate_constraint(const Net &w, const pfchem_options &o, Cell<R> &c, co
           const int j = w.mid(m, k);
           Jac[i][j] = R(w.mnu(m, k)) / c.pri_molal[j];
         }
+      } else if (type[i] == kConGas) {  // reaction.F90:1720-1751
+        const int g = mineral[i] - 1, ld = gas->paseq_ld;
+        R lnQK = -gas_logK[i] * R(kLOG_TO_LN);
+        if (gas->paseqh2oid && gas->paseqh2oid[g] > 0) lnQK = lnQK + R(gas->paseqh2ostoich[g]) * c.ln_act_h2o;
+        const int ns = gas->paseqspecid[g * (ld + 1)];
+        for (int k = 1; k <= ns; ++k) {
+          const int j = gas->paseqspecid[g * (ld + 1) + k] - 1;
+          lnQK = lnQK + R(gas->paseqstoich[g * ld + k - 1]) * rlog(c.pri_molal[j] * c.pri_act_coef[j]);
+        }
+        Res[i] = lnQK - rlog(R(conc[i]));
+        for (int k = 1; k <= ns; ++k) {
+          const int j = gas->paseqspecid[g * (ld + 1) + k] - 1;
+          Jac[i][j] = R(gas->paseqstoich[g * ld + k - 1]) / c.pri_molal[j];
+        }
+      } else if (type[i] == kConTotalSorb) {  // reaction.F90:1608-1614
+        Res[i] = c.total_sorb_eq[i] - total_conc[i];
+        for (int j = 0; j < N; ++j) Jac[i][j] = c.dtotal_sorb_eq[i][j];
       } else {  // charge balance (reaction.F90:1623-1634)
         Res[i] = 0;
         for (int j = 0; j < N; ++j) {
@@ -1644,6 +1672,11 @@ extern "C" {
 int pfo_equilibrate_constraints(const pfchem_network *net, const pfchem_options *opt, pfchem_cells *cells,
                                 const pfchem_constraint *con, int nthreads) {
   Net w = make_net(net, opt);
+  for (int j = 0; j < w.N; ++j)
+    if (con->type[j] == kConGas &&
+        (!con->mineral || con->mineral[j] < 1 || con->mineral[j] > con->npassive_gas || !con->paseqspecid ||
+         !con->paseqstoich || (opt->use_isothermal ? !con->paseqlogK : !con->paseqlogKcoef)))
+      return -1;
   const int64_t n = cells->ncells;
   std::atomic<int> bad{0};
   auto work = [&](int64_t k0, int64_t k1) {
@@ -1655,7 +1688,7 @@ int pfo_equilibrate_constraints(const pfchem_network *net, const pfchem_options 
       for (int j = 0; j < w.N; ++j) conc[j] = con->value[j * n + k];
       int its = 0;
       const int r = equilibrate_constraint(w, *opt, c, con->type, conc, &its, con->mineral,
-                                           con->max_iterations > 0 ? con->max_iterations : 10000);
+                                           con->max_iterations > 0 ? con->max_iterations : 10000, con);
       if (r) bad++;
       for (int j = 0; j < w.N; ++j) {
         cells->pri_molal[j * n + k] = c.pri_molal[j];

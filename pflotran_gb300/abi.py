@@ -169,9 +169,25 @@ def mineral_update(arrays, update_porosity=1, update_surface_area=1, surface_are
                          ptr("armor_mineral"), int(armor_flag), 0, ptr("armor_flag_out"))
 
 CONSTRAINT_TOTAL, CONSTRAINT_FREE, CONSTRAINT_CHARGE_BAL, CONSTRAINT_PH, CONSTRAINT_LOG, CONSTRAINT_MINERAL = 1, 2, 3, 4, 5, 6
+CONSTRAINT_GAS, CONSTRAINT_TOTAL_SORB = 7, 8
+PFCHEM_MAX_GAS_ROWS = 8
 
 
 class Constraint(C.Structure):
     """pfchem_constraint."""
     _fields_ = [("type", C.c_void_p), ("mineral", C.c_void_p), ("value", C.c_void_p),
-                ("max_iterations", C.c_int32), ("reserved", C.c_int32)]
+                ("max_iterations", C.c_int32), ("npassive_gas", C.c_int32), ("paseq_ld", C.c_int32),
+                ("reserved", C.c_int32), ("paseqspecid", C.c_void_p), ("paseqstoich", C.c_void_p),
+                ("paseqh2oid", C.c_void_p), ("paseqh2ostoich", C.c_void_p), ("paseqlogK", C.c_void_p),
+                ("paseqlogKcoef", C.c_void_p)]
+
+
+def constraint(types, values_ptr, spec_ids=None, max_iterations=0, gases=None):
+    """Constraint over numpy `types` / `spec_ids` (int32) and a values
+    pointer; `gases` the dict of GasTable.arrays() (kept alive by the caller)."""
+    def p(a):
+        return None if a is None else a.ctypes.data
+    g = gases or {}
+    return Constraint(p(types), p(spec_ids), values_ptr, int(max_iterations), int(g.get("n", 0)),
+                      int(g.get("ld", 0)), 0, p(g.get("specid")), p(g.get("stoich")), p(g.get("h2oid")),
+                      p(g.get("h2ostoich")), p(g.get("logK")), p(g.get("logKcoef")))

@@ -310,7 +310,7 @@ def rewrite_in_basis(rx_stoich, rx_logK, swapped, basis, what):
 
 
 def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, ion_exchange=None,
-                          surface_complexation=None, debye=None):
+                          surface_complexation=None, debye=None, gases=None):
     """ReactionNetwork for `primaries` (the database's basis or another one,
     rewritten as the module notes describe).
 
@@ -321,7 +321,9 @@ def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, 
     kinetic_minerals: {name: dict(rate_constant=mol/m^2/s, ...)} with the
       other add_kinetic_mineral keywords;
     ion_exchange: [(cations with selectivities [(name, k)], CEC)];
-    surface_complexation: [(site_density, [complex names], keywords)].
+    surface_complexation: [(site_density, [complex names], keywords)];
+    gases: names of passive gases (GAS constraint rows), their reactions
+      rewritten in the primaries like the minerals'.
     Log K is the 25 C value; the temperature fit is attached when the
     database has five or more temperatures with data."""
     from .network import ReactionNetwork
@@ -367,6 +369,13 @@ def network_from_database(db, primaries, secondary=None, kinetic_minerals=None, 
         kw = dict(kw)
         kw.setdefault("molar_vol", rx.molar_vol_cm3 * 1e-6)
         net.add_kinetic_mineral(n, {s: v for s, v in st if s != "H2O"}, logK=at25(lk, n), logKcoef=fit(lk), **kw)
+    for n in gases or []:
+        if not db.gases or n not in db.gases:
+            raise ValueError(f"gas {n} is not in the database")
+        rx = db.gases[n]
+        st, lk = rewrite_in_basis(rx.stoich, rx.logK, swapped, allowed, f"gas {n}")
+        net.add_passive_gas(n, {s: v for s, v in st if s != "H2O"}, logK=at25(lk, n), logKcoef=fit(lk),
+                            h2o=dict(st).get("H2O", 0.0))
     for cations, cec in (ion_exchange or []):
         net.add_ion_exchange(cations, cec)
     for site_density, complexes, kw in (surface_complexation or []):

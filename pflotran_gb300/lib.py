@@ -270,13 +270,15 @@ class ReactionStep(WarmStartMixin):
 
     def equilibrate_constraints(self, cells, types, values, minerals=None, max_iterations=0):
         """Constraint speciation of every cell of a device batch: `types`
-        (and 1-based `minerals`) per component, `values` a device tensor
-        (N, ncells).  Returns the number of cells that did not converge."""
+        and 1-based `minerals` (the constraint_spec_id: the kinetic mineral
+        of a MINERAL row, the network's passive gas of a GAS row) per
+        component, `values` a device tensor (N, ncells).  Returns the number
+        of cells that did not converge."""
         import numpy as np
         t = np.ascontiguousarray(types, np.int32)
         mn = None if minerals is None else np.ascontiguousarray(minerals, np.int32)
-        con = abi.Constraint(t.ctypes.data, None if mn is None else mn.ctypes.data, values.data_ptr(),
-                             int(max_iterations), 0)
+        gases = self.network.gas_table() if self.network.gases else None
+        con = abi.constraint(t, values.data_ptr(), mn, max_iterations, gases)
         s = cells.struct()
         return self._check(self._lib.pfchem_equilibrate_constraints(self._ctx, C.byref(s), C.byref(con)),
                            "pfchem_equilibrate_constraints")

@@ -60,6 +60,7 @@ class ReactionNetwork:
         self.minerals: list[_Rxn] = []
         self.ionx: list[dict] = []
         self.srfrxn: list[dict] = []
+        self.gases: list[_Rxn] = []
         self._tables = None
 
     # -- builders ---------------------------------------------------------
@@ -102,6 +103,32 @@ class ReactionNetwork:
                 flag = True
         self.srfrxn.append(dict(site_density=float(site_density), complexes=cx,
                                 surf_type=int(surf_type), to_surf=int(to_mineral), flag=flag))
+
+    def add_passive_gas(self, name, stoich, logK, logKcoef=None, h2o=0.0):
+        """A passive gas (reaction_gas_aux.F90 gas%paseq*): its reaction in the
+        primaries, log10 K at 25 C and the optional log K(T) fit.  Used by
+        GAS constraint rows only (no gas phase in the reaction step)."""
+        sp = list(stoich.keys())
+        self.gases.append(_Rxn(sp, [float(stoich[s]) for s in sp], float(logK), logKcoef, float(h2o),
+                               dict(name=name)))
+
+    def gas_id(self, name):
+        """1-based id of a passive gas (a GAS row's constraint_spec_id)."""
+        return [g.extra["name"] for g in self.gases].index(name) + 1
+
+    def gas_table(self):
+        """The passive-gas arrays of a pfchem_constraint (abi.constraint's
+        `gases`): paseqspecid (0:ld, n), paseqstoich (ld, n), h2o ids and
+        stoichiometries, log K and the log K(T) fit (5, n)."""
+        n = len(self.gases)
+        ld = max([len(g.species) for g in self.gases] + [1])
+        if ld > abi.PFCHEM_MAX_NNZ:
+            raise ValueError(f"a gas reaction has {ld} species (at most {abi.PFCHEM_MAX_NNZ})")
+        ids, nus = self._idtab(self.gases, ld, lambda rx: ([self.idx(q) for q in rx.species], rx.stoich))
+        return dict(n=n, ld=ld, specid=ids, stoich=nus,
+                    h2oid=_i32([1 if abs(g.h2o) > 0 else 0 for g in self.gases] or [0]),
+                    h2ostoich=_f64([g.h2o for g in self.gases] or [0.0]),
+                    logK=_f64([g.logK for g in self.gases] or [0.0]), logKcoef=_f64(self._coefs(self.gases)))
 
     # -- tables -------------------------------------------------------------
     @staticmethod

@@ -189,4 +189,7 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PFLOTRAN_SOURCE_DIR")
+    if not src:
+        sys.exit("usage: make_kat_fixtures.py <pflotran source tree> (or set PFLOTRAN_SOURCE_DIR)")
+    main(src)

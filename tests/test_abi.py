@@ -24,7 +24,9 @@ def test_library_builds_and_exports_header_symbols():
 
 @pytest.mark.parametrize("name,cls", [("pfchem_network", abi.Network), ("pfchem_options", abi.Options),
                                       ("pfchem_cells", abi.Cells), ("pfchem_stats", abi.Stats),
-                                      ("pfchem_launch", abi.Launch)])
+                                      ("pfchem_launch", abi.Launch), ("pfchem_constraint", abi.Constraint),
+                                      ("pfchem_mineral_update", abi.MineralUpdate),
+                                      ("pfchem_reaction_blocks_out", abi.ReactionBlocksOut)])
 def test_struct_layout_matches_header(tmp_path, name, cls):
     fields = [f[0] for f in cls._fields_]
     src = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{ROOT}/include/pfchem.h"', "int main(void){",

@@ -7,7 +7,8 @@ import pytest
 import kat
 from pflotran_gb300 import database
 
-REF_DB = "/root/reference/database/hanford.dat"
+# the reference tree is located by PFLOTRAN_SOURCE_DIR (the test is skipped without it)
+REF_DB = os.path.join(os.environ.get("PFLOTRAN_SOURCE_DIR", ""), "database", "hanford.dat")
 
 
 def test_network_from_database_matches_fixture_network(oracle, tmp_path):
