@@ -24,8 +24,8 @@ namespace pfchem {
 cudaError_t launch_react(const DevNet &n, const CellArgs &a, Scratch *scr, int grid, int block, int refill,
                          cudaStream_t st);
 cudaError_t launch_kinetic_state(const DevNet &n, const CellArgs &a, cudaStream_t st);
-cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const int32_t *type, const int32_t *mineral,
-                              const double *value, int max_its, Scratch *scr, cudaStream_t st);
+cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const pfchem_constraint &con, int max_its,
+                              Scratch *scr, cudaStream_t st);
 cudaError_t launch_mineral_properties(const CellArgs &a, int Nm, const pfchem_mineral_update &mu, int *flag_dev,
                                       cudaStream_t st);
 cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *res, double *jac, double *total,
@@ -834,19 +834,39 @@ int pfchem_equilibrate_constraints(pfchem_ctx *c, pfchem_cells *cl, const pfchem
   if (n.Nix + n.Nsr > 0 && (!cl->total_sorb_eq || (n.Nix && !cl->eqionx_ref_cation_sorbed_conc) ||
                             (n.Nsr && !cl->srfcplxrxn_free_site_conc)))
     return fail(c, -1, "sorption state arrays required");
+  int ngas_rows = 0;
   for (int j = 0; j < n.N; ++j) {
     const int t = con->type[j];
-    if (t < PFCHEM_CONSTRAINT_TOTAL || t > PFCHEM_CONSTRAINT_MINERAL)
+    if (t < PFCHEM_CONSTRAINT_TOTAL || t > PFCHEM_CONSTRAINT_TOTAL_SORB)
       return fail(c, -1, "component %d: unknown constraint type %d", j + 1, t);
     if (t == PFCHEM_CONSTRAINT_MINERAL && (!con->mineral || con->mineral[j] < 1 || con->mineral[j] > n.Nm))
       return fail(c, -1, "component %d: MINERAL row needs a kinetic mineral id in [1,%d]", j + 1, n.Nm);
+    if (t == PFCHEM_CONSTRAINT_TOTAL_SORB && n.Nix + n.Nsr == 0)
+      return fail(c, -1, "component %d: TOTAL_SORB row in a network without sorption", j + 1);
+    if (t == PFCHEM_CONSTRAINT_GAS) {
+      if (!con->mineral || con->mineral[j] < 1 || con->mineral[j] > con->npassive_gas)
+        return fail(c, -1, "component %d: GAS row needs a passive gas id in [1,%d]", j + 1, con->npassive_gas);
+      if (++ngas_rows > PFCHEM_MAX_GAS_ROWS)
+        return fail(c, -1, "more than %d GAS rows", PFCHEM_MAX_GAS_ROWS);
+      if (!con->paseqspecid || !con->paseqstoich || (n.isothermal ? !con->paseqlogK : !con->paseqlogKcoef))
+        return fail(c, -1, "GAS rows need paseqspecid, paseqstoich and %s",
+                    n.isothermal ? "paseqlogK" : "paseqlogKcoef");
+      if (con->paseq_ld < 1 || con->paseq_ld > PFCHEM_MAX_NNZ)
+        return fail(c, -1, "paseq_ld %d out of [1,%d]", con->paseq_ld, PFCHEM_MAX_NNZ);
+      const int g = con->mineral[j] - 1, ns = con->paseqspecid[g * (con->paseq_ld + 1)];
+      if (ns < 1 || ns > con->paseq_ld) return fail(c, -1, "gas %d: %d species", g + 1, ns);
+      for (int k = 1; k <= ns; ++k) {
+        const int id = con->paseqspecid[g * (con->paseq_ld + 1) + k];
+        if (id < 1 || id > n.N) return fail(c, -1, "gas %d: species id %d out of [1,%d]", g + 1, id, n.N);
+      }
+    }
   }
   cudaSetDevice(c->device);
   CellArgs a = device_args(cl, 1.0);
   if (a.ncells == 0) return 0;
   CUDA_TRY(c, cudaMemsetAsync(c->scratch, 0, sizeof(Scratch), c->stream));
-  cudaError_t le = launch_constraint(n, a, con->type, con->mineral, con->value,
-                                     con->max_iterations > 0 ? con->max_iterations : 10000, c->scratch, c->stream);
+  cudaError_t le = launch_constraint(n, a, *con, con->max_iterations > 0 ? con->max_iterations : 10000, c->scratch,
+                                     c->stream);
   if (le != cudaSuccess) return fail(c, -2, "constraint launch: %s", cudaGetErrorString(le));
   Scratch h;
   CUDA_TRY(c, cudaMemcpyAsync(&h, c->scratch, sizeof(Scratch), cudaMemcpyDeviceToHost, c->stream));

@@ -1100,8 +1100,15 @@ static cudaError_t launch_blocks_t(const DevNet &n, const CellArgs &a, const Blo
 // d total/d ln m in the shared-memory system).
 struct ConstraintRows {
   int8_t type[PFCHEM_MAX_PRI];
-  int8_t mineral[PFCHEM_MAX_PRI];  // 0-based kinetic mineral of MINERAL rows
+  int8_t mineral[PFCHEM_MAX_PRI];  // 0-based kinetic mineral of MINERAL rows, gas reaction of GAS rows
+  int8_t gn[PFCHEM_MAX_GAS_ROWS];  // GAS reaction g: species count, 0-based primaries, coefficients
+  int8_t gid[PFCHEM_MAX_GAS_ROWS][PFCHEM_MAX_NNZ];
+  double gnu[PFCHEM_MAX_GAS_ROWS][PFCHEM_MAX_NNZ];
+  double gh2o[PFCHEM_MAX_GAS_ROWS];     // H2O coefficient (0 where H2O takes no part)
+  double glogK[PFCHEM_MAX_GAS_ROWS];    // log10 K (isothermal)
+  double gcoef[PFCHEM_MAX_GAS_ROWS][5]; // log K(T) fit
   int32_t max_its;
+  int32_t any_sorb_row;
   const double *value;             // (N, ncells)
 };
 
@@ -1130,13 +1137,23 @@ __global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ 
   L.v_t = 0.0;
   L.jac_mnrl = 0.0;
   const double molar_to_molal = 1000.0 / a.den[cell];
-  double freec[S::NP], totc[S::NP], val[S::NP], res[S::NP], prev[S::NP];
+  double freec[S::NP], totc[S::NP], val[S::NP], res[S::NP], prev[S::NP], gb[S::NP];
   for (int j = 0; j < N; ++j) {
     val[j] = con.value[j * nc + cell];
     freec[j] = 1e-9;
     totc[j] = 0.0;
+    gb[j] = 0.0;
     switch (con.type[j]) {
-      case PFCHEM_CONSTRAINT_TOTAL: totc[j] = val[j]; break;
+      case PFCHEM_CONSTRAINT_TOTAL:
+      case PFCHEM_CONSTRAINT_TOTAL_SORB: totc[j] = val[j]; break;
+      case PFCHEM_CONSTRAINT_GAS: {  // log10 partial pressure when <= 0 (reaction.F90:1531-1535)
+        if (val[j] <= 0.0) val[j] = pow(10.0, val[j]);
+        const int g = con.mineral[j];
+        const double tk = L.temp + 273.15;
+        const double lk = n.isothermal ? con.glogK[g] : logK_at(con.gcoef[g], log(tk), tk, 1.0 / tk);
+        gb[j] = -lk * kLOG_TO_LN;
+        break;
+      }
       case PFCHEM_CONSTRAINT_FREE:
       case PFCHEM_CONSTRAINT_CHARGE_BAL:
       case PFCHEM_CONSTRAINT_MINERAL: freec[j] = val[j] * molar_to_molal; break;
@@ -1159,6 +1176,30 @@ __global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ 
       for (int j = 0; j < N; ++j) I += n.Z2p[j] * L.m[j];
       for (int i = 0; i < n.Nc; ++i) I += n.cZ2[i] * L.C[i];
       activity(n, L, 0.5 * I);
+    }
+    // sorbed totals and d/dm of TOTAL_SORB rows: one evaluation with the
+    // sorption weights, the sorption warm starts then put back so that the
+    // aqueous evaluation below runs the same inner iterations
+    double sres[S::NP], sjac[S::NP][S::NP];
+    if (con.any_sorb_row) {
+      double ix0[S::NIX], sr0[S::NSR];
+      for (int r = 0; r < n.Nix; ++r) ix0[r] = L.ixref[r];
+      for (int r = 0; r < n.Nsr; ++r) sr0[r] = L.srfree[r];
+      L.jac_aq = 0.0;
+      L.v_t = 1.0;
+      if (evaluate<S, true>(n, L, J, js, n.jac_exact)) {
+        status = 1;
+        break;
+      }
+      for (int i = 0; i < N; ++i)
+        if (con.type[i] == PFCHEM_CONSTRAINT_TOTAL_SORB) {
+          sres[i] = L.S_[i];
+          for (int k = 0; k < N; ++k) sjac[i][k] = J[(i * N + k) * js] / L.m[k];
+        }
+      for (int r = 0; r < n.Nix; ++r) L.ixref[r] = ix0[r];
+      for (int r = 0; r < n.Nsr; ++r) L.srfree[r] = sr0[r];
+      L.jac_aq = L.den_L;
+      L.v_t = 0.0;
     }
     if (evaluate<S, true>(n, L, J, js, n.jac_exact)) {
       status = 1;
@@ -1204,6 +1245,25 @@ __global__ void __launch_bounds__(32) constraint_kernel(const __grid_constant__ 
           }
           break;
         }
+        case PFCHEM_CONSTRAINT_GAS: {  // reaction.F90:1720-1751
+          const int g = con.mineral[i];
+          double lnQK = gb[i] + con.gh2o[g] * L.lnaw;
+          for (int k = 0; k < con.gn[g]; ++k) {
+            const int j = con.gid[g][k];
+            lnQK += con.gnu[g][k] * log(L.m[j] * L.gp[j]);
+          }
+          res[i] = lnQK - log(val[i]);
+          for (int k = 0; k < N; ++k) J[(i * N + k) * js] = 0.0;
+          for (int k = 0; k < con.gn[g]; ++k) {
+            const int j = con.gid[g][k];
+            J[(i * N + j) * js] = con.gnu[g][k] / L.m[j];
+          }
+          break;
+        }
+        case PFCHEM_CONSTRAINT_TOTAL_SORB:  // reaction.F90:1608-1614
+          res[i] = sres[i] - totc[i];
+          for (int k = 0; k < N; ++k) J[(i * N + k) * js] = sjac[i][k];
+          break;
         default: {  // FREE, LOG, PH: identity row
           if (con.type[i] == PFCHEM_CONSTRAINT_PH) L.m[i] = pow(10.0, -val[i]) / L.gp[i];
           res[i] = 0.0;
@@ -1410,15 +1470,29 @@ cudaError_t launch_reaction_blocks(const DevNet &n, const CellArgs &a, double *r
   }
 }
 
-cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const int32_t *type, const int32_t *mineral,
-                              const double *value, int max_its, Scratch *scr, cudaStream_t st) {
+cudaError_t launch_constraint(const DevNet &n, const CellArgs &a, const pfchem_constraint &con, int max_its,
+                              Scratch *scr, cudaStream_t st) {
   ConstraintRows c{};
+  int ngas = 0;
   for (int j = 0; j < n.N; ++j) {
-    c.type[j] = (int8_t)type[j];
-    c.mineral[j] = (int8_t)(mineral && mineral[j] > 0 ? mineral[j] - 1 : 0);
+    c.type[j] = (int8_t)con.type[j];
+    c.mineral[j] = (int8_t)(con.mineral && con.mineral[j] > 0 ? con.mineral[j] - 1 : 0);
+    if (con.type[j] == PFCHEM_CONSTRAINT_TOTAL_SORB) c.any_sorb_row = 1;
+    if (con.type[j] == PFCHEM_CONSTRAINT_GAS) {  // the row's gas reaction, compacted (ids checked by the caller)
+      const int g = con.mineral[j] - 1, ld = con.paseq_ld, q = ngas++;
+      c.mineral[j] = (int8_t)q;
+      c.gn[q] = (int8_t)con.paseqspecid[g * (ld + 1)];
+      for (int k = 0; k < c.gn[q]; ++k) {
+        c.gid[q][k] = (int8_t)(con.paseqspecid[g * (ld + 1) + 1 + k] - 1);
+        c.gnu[q][k] = con.paseqstoich[g * ld + k];
+      }
+      c.gh2o[q] = (con.paseqh2oid && con.paseqh2oid[g] > 0) ? con.paseqh2ostoich[g] : 0.0;
+      c.glogK[q] = con.paseqlogK ? con.paseqlogK[g] : 0.0;
+      for (int k = 0; k < 5; ++k) c.gcoef[q][k] = con.paseqlogKcoef ? con.paseqlogKcoef[5 * g + k] : 0.0;
+    }
   }
   c.max_its = max_its;
-  c.value = value;
+  c.value = con.value;
   switch (size_class(n)) {
     case 0: return launch_constraint_t<SizesS>(n, a, c, scr, st);
     case 1: return launch_constraint_t<SizesM>(n, a, c, scr, st);

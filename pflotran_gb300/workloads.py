@@ -166,6 +166,32 @@ def add_rate_prefactors(net):
     return net
 
 
+def add_passive_gases(net, seed=0):
+    """Passive gases for GAS constraint rows (reaction.F90:1720-1751), in
+    place: CO2(g) = H+ + HCO3- - H2O (log K -7.8136 at 25 C) when the network
+    has those primaries, else two seeded gases, each the product of two or
+    three primaries with log K in [0, 5].
+    log K(T) is linear in T_K with a seeded +-0.3 offset at 60 C.  Returns net."""
+    rng = np.random.default_rng(seed + 104729)
+
+    def coef(lk):
+        d = 0.3 if rng.random() < 0.5 else -0.3
+        b = d / (333.15 - 298.15)
+        return (0.0, lk - b * 298.15, b, 0.0, 0.0)
+
+    if "H+" in net.pri_names and "HCO3-" in net.pri_names:
+        net.add_passive_gas("CO2(g)", {"H+": 1.0, "HCO3-": 1.0}, -7.8136, logKcoef=coef(-7.8136), h2o=-1.0)
+    else:
+        pn = net.pri_names
+        for g in range(2):
+            k = 2 + g
+            ids = rng.choice(len(pn), size=min(k, len(pn)), replace=False)
+            st = {pn[i]: 1.0 for i in ids}  # partial pressures below 1 bar (activities < 1)
+            lk = float(rng.uniform(0.0, 5.0))
+            net.add_passive_gas(f"G{g + 1}(g)", st, lk, logKcoef=coef(lk))
+    return net
+
+
 # ---------------------------------------------------------------------------
 # forward speciation for input generation (torch, float64, CPU or CUDA)
 

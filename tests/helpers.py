@@ -39,8 +39,9 @@ def compare(net, gpu, ref, tol=1e-10, mask=None):
 def constraint_problem(oracle, net, opt, cells, rows):
     """Constraint rows and per-cell values that describe each cell's own
     equilibrium state: rows maps component -> kind ('total', 'ph', 'log',
-    'free', 'mineral:<k>', 'charge'); unspecified components are 'total'.
-    Returns (types, minerals, values[N, ncells])."""
+    'free', 'mineral:<k>', 'charge', 'gas:<k>' (partial pressure [bar]),
+    'loggas:<k>' (its log10), 'sorb' (sorbed total)); unspecified components
+    are 'total'.  Returns (types, spec ids, values[N, ncells])."""
     n, N = cells.ncells, net.N
     blocks = oracle.reaction_blocks(net.as_struct(), opt, cells.copy())
     m = cells.pri_molal.reshape(N, n)
@@ -60,7 +61,29 @@ def constraint_problem(oracle, net, opt, cells, rows):
             types[j], values[j] = abi.CONSTRAINT_CHARGE_BAL, molar[j]
         elif kind.startswith("mineral:"):
             types[j], minerals[j], values[j] = abi.CONSTRAINT_MINERAL, int(kind.split(":")[1]), molar[j]
+        elif kind.startswith(("gas:", "loggas:")):
+            g = int(kind.split(":")[1])
+            rx = net.gases[g - 1]
+            act = np.array([oracle.activity_lag(net.as_struct(), float(I), N, net.Nc)[0] for I in cells.ionic_strength]).T
+            lnQK = -rx.logK * 2.30258509299 + sum(nu * np.log(m[net.idx(q)] * act[net.idx(q)])
+                                                 for q, nu in zip(rx.species, rx.stoich))
+            p = np.exp(lnQK)
+            types[j], minerals[j] = abi.CONSTRAINT_GAS, g
+            values[j] = p if kind.startswith("gas:") else np.log10(p)
+        elif kind == "sorb":
+            types[j], values[j] = abi.CONSTRAINT_TOTAL_SORB, blocks["total_sorb"][j]
     return types, minerals, np.ascontiguousarray(values)
+
+
+def gas_sorb_rows(net):
+    """Constraint rows with GAS rows on a species of each of the network's
+    gas reactions (the second in log10 form) and a TOTAL_SORB row on an
+    exchanged cation; the rest TOTAL."""
+    rows = {net.ionx[0]["ids"][1]: "sorb"}
+    for g, rx in enumerate(net.gases):
+        j = next(net.idx(q) for q in rx.species if net.idx(q) not in rows)
+        rows[j] = ("gas:" if g == 0 else "loggas:") + str(g + 1)
+    return rows
 
 
 def truth_solve(oracle, net, opt, cells, dt, start, nthreads=None):

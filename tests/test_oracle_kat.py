@@ -134,6 +134,79 @@ def test_constraint_rows_are_satisfied(oracle):
     assert np.abs(lnQK).max() < 1e-6
 
 
+def test_constraint_gas_and_sorbed_rows_are_satisfied(oracle):
+    """GAS rows (reaction.F90:1720-1751: the gas reaction's ln QK equals the
+    log of the partial pressure; a value <= 0 is log10 of it) and a
+    TOTAL_SORB row (:1608-1614): the solution meets every row and is the
+    cells' own state; log10 and plain partial pressures give the same answer."""
+    from pflotran_gb300 import abi, workloads
+    from helpers import constraint_problem, gas_sorb_rows
+    net, _, cells, dt = workloads.synthetic_cells(64, seed=43)
+    workloads.add_passive_gases(net)
+    copt = workloads.default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                                     max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    rows = gas_sorb_rows(net)
+    types, spec, values = constraint_problem(oracle, net, copt, cells, rows)
+    assert (types == abi.CONSTRAINT_GAS).sum() == 2 and (types == abi.CONSTRAINT_TOTAL_SORB).sum() == 1
+    out = cells.copy()
+    out.sec_molal = np.zeros(net.Nc * cells.ncells)
+    gases = net.gas_table()
+    bad = oracle.equilibrate_constraints(net.as_struct(), copt, out, types, values, spec, gases=gases)
+    assert bad == 0, np.bincount(out.status)
+    N, n = net.N, cells.ncells
+    m = out.pri_molal.reshape(N, n)
+    tot = out.total_out.reshape(N, n)
+    sorb = out.total_sorb_eq.reshape(N, n)
+    for j in range(N):
+        if types[j] == abi.CONSTRAINT_TOTAL:
+            assert np.abs(tot[j] - values[j]).max() <= 1e-10 * np.abs(values[j]).max()
+        if types[j] == abi.CONSTRAINT_TOTAL_SORB:
+            np.testing.assert_allclose(sorb[j], values[j], rtol=1e-10)
+    gp = np.array([oracle.activity_lag(net.as_struct(), float(I), N, net.Nc)[0] for I in out.ionic_strength]).T
+    for j in np.flatnonzero(types == abi.CONSTRAINT_GAS):
+        rx = net.gases[spec[j] - 1]
+        lnQK = -rx.logK * 2.30258509299 + sum(nu * np.log(m[net.idx(q)] * gp[net.idx(q)])
+                                             for q, nu in zip(rx.species, rx.stoich))
+        p = values[j] if values[j].max() > 0 else 10.0 ** values[j]
+        assert np.abs(lnQK - np.log(p)).max() < 1e-8
+    # the rows describe each cell's own equilibrium state
+    np.testing.assert_allclose(m, cells.pri_molal.reshape(N, n), rtol=1e-6)
+    # the log10 form of a partial pressure
+    j2 = next(j for j in np.flatnonzero(types == abi.CONSTRAINT_GAS) if values[j].max() <= 0)
+    v2 = values.copy()
+    v2[j2] = 10.0 ** values[j2]
+    out2 = cells.copy()
+    out2.sec_molal = np.zeros(net.Nc * cells.ncells)
+    assert oracle.equilibrate_constraints(net.as_struct(), copt, out2, types, v2, spec, gases=gases) == 0
+    np.testing.assert_allclose(out2.pri_molal, out.pri_molal, rtol=1e-12)
+
+
+def test_constraint_gas_row_with_database_gas(oracle):
+    """CO2(g) read from a database's gas block and rewritten in the
+    primaries (H+ + HCO3- - H2O): the calcite water of a column's initial
+    condition (free H+, HCO3- from 1e-3 bar CO2(g), Ca++ at calcite
+    saturation) converges and meets its gas row."""
+    from pflotran_gb300 import abi, workloads
+    net, _, cells, dt = workloads.calcite_cells(4, seed=44)
+    workloads.add_passive_gases(net)
+    assert net.gases[0].extra["name"] == "CO2(g)" and net.gases[0].h2o == -1.0
+    copt = workloads.default_options(use_isothermal=1, residual_tol_kind=abi.RESIDUAL_ABSOLUTE,
+                                     max_relative_change_tolerance=1e-6, max_residual_tolerance=1e-12)
+    n = cells.ncells
+    types = np.array([abi.CONSTRAINT_FREE, abi.CONSTRAINT_GAS, abi.CONSTRAINT_MINERAL], np.int32)
+    spec = np.array([0, 1, 1], np.int32)
+    values = np.array([[1e-8] * n, [1e-3] * n, [5e-4] * n])
+    out = cells.copy()
+    out.sec_molal = np.zeros(net.Nc * n)
+    assert oracle.equilibrate_constraints(net.as_struct(), copt, out, types, values, spec,
+                                          gases=net.gas_table()) == 0
+    m = out.pri_molal.reshape(3, n)
+    gp = np.array([oracle.activity_lag(net.as_struct(), float(I), 3, net.Nc)[0] for I in out.ionic_strength]).T
+    lnQK = 7.8136 * 2.30258509299 + np.log(m[0] * gp[0]) + np.log(m[1] * gp[1])
+    assert np.abs(lnQK - np.log(1e-3)).max() < 1e-8
+    np.testing.assert_allclose(m[0] * cells.den_kg[:n] * 1e-3, 1e-8, rtol=1e-12)
+
+
 def test_surface_complexation_1_gold(oracle):
     """surface-complexation-1 (time 0): constraint speciation with pH and
     charge-balance rows + one equilibrium surface-complexation site
