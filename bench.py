@@ -200,13 +200,14 @@ def cpu_baseline(net, opt, cells, dt, sample):
     return cb, idx, sub, ref
 
 
-def parity_block(net, opt, dt, sub, ref, gpu_sub, truth, alt_guess=None):
+def parity_block(net, opt, dt, sub, ref, gpu_sub, truth, alt=None):
     """GPU against the oracle on the sample: error statement and the per-cell
-    bar against the root."""
+    bar against the root (and, given `alt`, the oracle's answer from another
+    starting guess)."""
     from oracle import parity
     both = (ref.status == 0) & (gpu_sub.status == 0)
     st = parity.error_statement(net, gpu_sub, ref, both)
-    bar = parity.per_cell_bar(net, gpu_sub, ref, truth, 1e-10, both & (truth.status == 0))
+    bar = parity.per_cell_bar(net, gpu_sub, ref, truth, 1e-10, both & (truth.status == 0), alt=alt)
     out = {"cells": int(both.sum()), "gpu_nonconverged": int((gpu_sub.status != 0).sum()),
            "oracle_nonconverged": int((ref.status != 0).sum()),
            "same_iterations": float(np.mean(ref.iterations[both] == gpu_sub.iterations[both])) if both.any() else None}
@@ -693,7 +694,7 @@ def main():
                "plain": parity_block(net, opt, dt, sub, ref, g_plain.subset(idx, net), truth)}
         if warm is not None and pred_sample is not None:
             ref_w = parity.solve(net, opt, dt, sub, 0, alt_guess=pred_sample.ravel())
-            par["warm"] = parity_block(net, opt, dt, sub, ref_w, g.subset(idx, net), truth)
+            par["warm"] = parity_block(net, opt, dt, sub, ref_w, g.subset(idx, net), truth, alt=ref)
             both = (ref.status == 0) & (g.subset(idx, net).status == 0)
             par["warm_vs_plain_oracle"] = parity.error_statement(net, g.subset(idx, net), ref, both)
         for mode, ge in exact_out.items():

@@ -109,20 +109,40 @@ def truth_solve(net, opt, dt, cells, start, nthreads=None):
     return solve(net, truth_options(opt), dt, cells, precision=1, nthreads=nthreads, alt_guess=start.pri_molal)
 
 
-def per_cell_bar(net, x, ref, truth, tol=1e-10, mask=None):
+def per_cell_bar(net, x, ref, truth, tol=1e-10, mask=None, alt=None):
     """Per cell and quantity (totals, volume fractions, rates): x is within
     `tol` of the oracle `ref`, or no farther from the root `truth` than `ref`
-    itself is (floor `tol`).  The second branch covers ill-conditioned cells,
+    itself is (floor `tol`), or -- given `alt`, the oracle's answer for the
+    same cell from another starting guess -- no farther from `ref` than
+    `alt` is.  The second and third branches cover ill-conditioned cells,
     where two Newton paths that both stop at the 1e-12 residual test (a
     rounding difference in the stopping iteration, a different starting
-    guess) land up to the tolerance x the conditioning apart.  Returns
-    {quantity: (pass mask, errors vs ref, errors vs truth, ref vs truth)};
-    cells outside `mask` pass."""
+    guess) land up to the tolerance x the conditioning apart: the third
+    measures that spread on the oracle itself.  Returns {quantity: (pass
+    mask, errors vs ref, errors vs truth, ref vs truth)}; cells outside
+    `mask` pass."""
     exr, ext, ert = cell_errors(net, x, ref), cell_errors(net, x, truth), cell_errors(net, ref, truth)
+    spread = cell_errors(net, alt, ref) if alt is not None else None
     if mask is None:
         mask = np.ones(ref.ncells, bool)
     out = {}
     for q in exr:
         ok = (exr[q] <= tol) | (ext[q] <= np.maximum(tol, ert[q]))
+        if spread is not None:
+            ok |= exr[q] <= spread[q]
         out[q] = (ok | ~mask, exr[q], ext[q], ert[q])
     return out
+
+
+def bar_failures(net, x, ref, truth, bar, alt=None):
+    """The cells a per_cell_bar result fails, one line each: quantity, cell,
+    errors vs the oracle / x vs root / oracle vs root (/ oracle spread),
+    iterations of x and of the oracle."""
+    spread = cell_errors(net, alt, ref) if alt is not None else None
+    lines = []
+    for q, (ok, exr, ext, ert) in bar.items():
+        for c in np.flatnonzero(~ok):
+            s = f" spread {spread[q][c]:.3e}" if spread is not None else ""
+            lines.append(f"{q} cell {c}: vs oracle {exr[c]:.3e}, vs root {ext[c]:.3e}, oracle vs root "
+                         f"{ert[c]:.3e}{s}, iterations {int(x.iterations[c])}/{int(ref.iterations[c])}")
+    return lines

@@ -34,7 +34,8 @@ namespace pfchem {
 cudaError_t umma_prepare();
 bool umma_supports(int N, int K, bool w_kn);
 cudaError_t umma_linear(cudaStream_t st, const __nv_bfloat16 *X, long long rows, int K, const __nv_bfloat16 *W, int N,
-                        bool w_kn, const float *bias, float *Cf, __nv_bfloat16 *Cb, int epi, int *err, int sms);
+                        bool w_kn, const float *bias, float *Cf, __nv_bfloat16 *Cb, int epi, int *err, int sms,
+                        __nv_bfloat16 *bpk);
 constexpr int kUmmaGeluE = 0, kUmmaLinearE = 1;  // umma_linear epilogues
 
 constexpr int kFeat = 16;    // input features
@@ -515,6 +516,7 @@ struct Surrogate {
   // fused one-kernel inference), 1 = tcgen05.mma with tensor-memory accumulators
   int backend = 0;
   int *uerr = nullptr;      // set by a tcgen05 kernel whose wait ran out
+  bf16 *ubpk = nullptr;     // a layer's weights packed for the tcgen05 kernels (256 x 256)
   int sms = 0;
 };
 constexpr int kSplits = 16;  // weight-gradient GEMMs: K = batch rows split 16 ways
@@ -565,9 +567,10 @@ void forward(Surrogate *s, long long rows, cudaStream_t st, bool keep) {
     const float *b = s->w + s->boff[l];
     if (s->backend == 1 && umma_supports(Nn, K, true)) {
       if (l < kLayers - 1)
-        umma_linear(st, in, rows, K, W, Nn, true, b, keep ? s->z[l] : nullptr, s->hb[l], kUmmaGeluE, s->uerr, s->sms);
+        umma_linear(st, in, rows, K, W, Nn, true, b, keep ? s->z[l] : nullptr, s->hb[l], kUmmaGeluE, s->uerr, s->sms,
+                    s->ubpk);
       else
-        umma_linear(st, in, rows, K, W, Nn, true, b, s->y, nullptr, kUmmaLinearE, s->uerr, s->sms);
+        umma_linear(st, in, rows, K, W, Nn, true, b, s->y, nullptr, kUmmaLinearE, s->uerr, s->sms, s->ubpk);
     } else if (l < kLayers - 1) {
       gemm<kEpiAct>(st, in, K, 1, W, Nn, 1, (int)rows, Nn, K, b, keep ? s->z[l] : nullptr, s->hb[l], Nn, 1);
     } else {
@@ -597,7 +600,8 @@ void backward(Surrogate *s, long long rows, cudaStream_t st) {
       // dH_{l-1} [rows x K] = dZ [rows x N] . W^T, W stored [K x N]
       const bf16 *W = s->wb + s->woff[l];
       if (s->backend == 1 && umma_supports(K, Nn, false))
-        umma_linear(st, dZb, rows, Nn, W, K, false, nullptr, s->dz[l - 1], nullptr, kUmmaLinearE, s->uerr, s->sms);
+        umma_linear(st, dZb, rows, Nn, W, K, false, nullptr, s->dz[l - 1], nullptr, kUmmaLinearE, s->uerr, s->sms,
+                    s->ubpk);
       else
         gemm<kEpiF32>(st, dZb, Nn, 1, W, 1, Nn, (int)rows, K, Nn, nullptr, s->dz[l - 1], nullptr, K, 0);
       // through the GELU of layer l-1: dZ_{l-1} = dH * GELU'(Z_{l-1}) (in place in dz)
@@ -639,6 +643,7 @@ Surrogate *surrogate_create(int N, uint64_t seed, std::string *err) {
   if (e == cudaSuccess) e = cudaMalloc(&s->tmu, 2 * kOut * sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->loss, sizeof(float));
   if (e == cudaSuccess) e = cudaMalloc(&s->uerr, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&s->ubpk, 256 * 256 * sizeof(bf16));
   if (e == cudaSuccess) e = cudaMemset(s->uerr, 0, sizeof(int));
   if (e == cudaSuccess) e = umma_prepare();
   if (e != cudaSuccess) {
@@ -677,6 +682,7 @@ void surrogate_destroy(Surrogate *s) {
   cudaFree(s->wpk);
   cudaFree(s->ws);
   cudaFree(s->uerr);
+  cudaFree(s->ubpk);
   cudaFree(s->fmu);
   cudaFree(s->tmu);
   cudaFree(s->loss);
