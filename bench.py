@@ -54,8 +54,8 @@ METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start v
 UNIT = "cell solves/s"
 NCELLS = 2_097_152
 # DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
-# on 524,288 cells of the same workload (561.5 MB read + 290.3 MB written)
-TRAFFIC_BYTES_PER_CELL = (561539840 + 290312704) / 524288
+# on 524,288 cells of the same workload (568.3 MB read + 314.2 MB written)
+TRAFFIC_BYTES_PER_CELL = (568272896 + 314241024) / 524288
 SAMPLE_SEED = 12345
 
 
@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--train-samples", type=int, default=8_388_608)
     p.add_argument("--epochs", type=int, default=12)
     p.add_argument("--plain-only", action="store_true")
+    p.add_argument("--mlp-backend", choices=("mma.sync", "tcgen05"), default="mma.sync",
+                   help="tensor-core path of the warm-start MLP (training and the step's inference)")
     p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
                    help="also time the step with the exact Newton Jacobian")
     p.add_argument("--reference-path", action=argparse.BooleanOptionalAction, default=True,
@@ -397,17 +399,19 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
+    from pflotran_gb300 import abi as _abi
     from pflotran_gb300 import work
     from pflotran_gb300.cells import CellBatch
     from pflotran_gb300.lib import ReactionStep
 
     net, opt, host, dt = make_workload(args.ncells, device=f"cuda:{local}", rank=rank)
     if args.jacobian == "exact":
-        from pflotran_gb300 import abi as _abi
         opt.jacobian = _abi.JACOBIAN_EXACT
         args.exact_jacobian = False  # the headline already is the exact-Jacobian run
     n = host.ncells
     step = ReactionStep(net, opt, device=local)
+    mlp_backend = _abi.MLP_TCGEN05 if args.mlp_backend == "tcgen05" else _abi.MLP_MMA_SYNC
+    step.surrogate_backend(mlp_backend)
     pristine = host.to_device()
     dev = pristine.copy()
     tune = None
@@ -484,6 +488,7 @@ def main():
         del pred
         # inference alone: features + the fused four-layer MLP (+ weight
         # packing and the guess copy) over all cells, best of 3 synchronous calls
+        step.surrogate_backend(_abi.MLP_MMA_SYNC)
         inf_ms = []
         for _ in range(3):
             torch.cuda.synchronize()
@@ -498,7 +503,6 @@ def main():
                      "peak_source": "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)",
                      "backend": "mma.sync fused one-kernel inference"}
         # the same inference on the tcgen05 path (layer by layer, TMEM accumulators)
-        from pflotran_gb300 import abi as _abi
         try:
             step.surrogate_backend(_abi.MLP_TCGEN05)
             t_ms = []
@@ -513,7 +517,8 @@ def main():
         except Exception as e:
             inference["tcgen05"] = {"error": str(e)[:200]}
         finally:
-            step.surrogate_backend(_abi.MLP_MMA_SYNC)
+            step.surrogate_backend(mlp_backend)
+        inference["backend_in_step"] = args.mlp_backend
         step.surrogate_enable(True)
         warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit, inference=inference,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),
@@ -542,8 +547,7 @@ def main():
     exact_out = {}
     if args.exact_jacobian:
         # the same step with the exact Newton Jacobian (same equations and root)
-        from pflotran_gb300 import abi
-        step.set_options(_opts(opt, jacobian=abi.JACOBIAN_EXACT))
+        step.set_options(_opts(opt, jacobian=_abi.JACOBIAN_EXACT))
         exact = {}
         for mode in (("plain", "warm") if warm is not None else ("plain",)):
             if warm is not None:
@@ -631,7 +635,8 @@ def main():
                  "speedup_vs_plain": value / plain["value"],
                  "alt_guess_used_frac": float(np.mean(head["alt"])) / n,
                  "surrogate": {"arch": "16-256-256-256-12 GELU MLP, BF16 weights/activations, FP32 accumulate "
-                                       "(mma.sync m16n8k16)",
+                                       + ("(tcgen05.mma, TMEM accumulators)" if args.mlp_backend == "tcgen05"
+                                          else "(mma.sync m16n8k16)"),
                                "train_samples": int(r.samples), "epochs": args.epochs, "steps": int(r.steps),
                                "first_loss": r.first_loss, "final_loss": r.final_loss,
                                "train_ms_device": r.train_ms, "data_generation_s": warm["t_gen"],
@@ -658,7 +663,8 @@ def main():
         "iteration_histogram": np.bincount(g.iterations).tolist(),
         # per step: prologue + persistent solve; the warm start adds the weight
         # packing (one launch per layer) and the fused MLP inference
-        "gpu_launches": args.steps * (2 if warm is None else 2 + 4 + 1),
+        "gpu_launches": args.steps * (2 if warm is None else 2 + (4 + 1 if args.mlp_backend == "mma.sync" else
+                                                                   1 + ((n + 262143) // 262144) * 10)),
         "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": probe, "unit": "TFLOP/s",
                      "frac": achieved_tflops / probe if probe else None,
                      "traffic": TRAFFIC_BYTES_PER_CELL * n,

@@ -6,13 +6,13 @@
 // C[rows x N] = X[rows x K] . B + bias, with B the layer's weights: stored
 // K x N (n contiguous: the forward pass, X W) or N x K (k contiguous: the
 // backward pass, dZ W^T), packed by a small kernel into the operand layout
-// first.  A persistent grid of one CTA (8 warps) per SM keeps the whole B (up
+// first.  A persistent grid of one CTA (16 warps) per SM keeps the whole B (up
 // to 256 x 256 BF16, 128 KB) in shared memory and streams 128-row tiles of X
 // through it: cp.async stages a tile into shared memory, K/16 MMAs of
 // 128 x N x 16 accumulate into N tensor-memory columns, and while the next
-// tile's copies are in flight the 8 warps read the accumulator (warp w: rows
-// 32*(w%4).., half w/4 of the columns, 16 columns at a time) to add the bias,
-// apply GELU and store BF16 and/or FP32.
+// tile's copies are in flight the 16 warps read the accumulator (warp w: rows
+// 32*(w%4).., a quarter w/4 of the columns, 16 columns at a time) to add the
+// bias (held in shared memory), apply GELU and store BF16 and/or FP32.
 //
 // Operand layout: the canonical K-major layout without swizzle -- core
 // matrices of 8 rows x 16 bytes stored contiguously, the next core matrix
@@ -81,7 +81,7 @@ __device__ __forceinline__ void u_cp16(uint32_t dst, const void *src, uint32_t b
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(bytes) : "memory");
 }
 
-constexpr int kUThreads = 256;  // 8 warps: loads and epilogue; thread 0 issues the MMAs
+constexpr int kUThreads = 512;  // 16 warps: loads and epilogue; thread 0 issues the MMAs
 
 // The A tile of rows [m0, m0 + 128) into shared memory with cp.async, zero
 // rows past `rows`.  One warp instruction moves 8 rows x 4 chunks (K >= 32)
@@ -115,9 +115,11 @@ __global__ void __launch_bounds__(kUThreads, 1) umma_linear_kernel(const bf16u *
   extern __shared__ __align__(1024) uint8_t sm[];
   uint8_t *Bs = sm;
   uint8_t *As = sm + BBYTES;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + BBYTES + ABYTES);
-  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + BBYTES + ABYTES + 8);
+  float *bias_s = reinterpret_cast<float *>(sm + BBYTES + ABYTES);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(sm + BBYTES + ABYTES + N * 4);
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(sm + BBYTES + ABYTES + N * 4 + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int c = tid; c < N; c += kUThreads) bias_s[c] = bias ? bias[c] : 0.f;
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(u_smem(tslot)), "n"(NCOL)
                  : "memory");
@@ -135,10 +137,11 @@ __global__ void __launch_bounds__(kUThreads, 1) umma_linear_kernel(const bf16u *
   constexpr uint32_t idesc = u_idesc(TM, N);
   uint32_t phase = 0;
   bool ok = true;
-  // epilogue split: warp w reads TMEM lanes 32*(w%4).. (rows) and half w/4 of the columns
-  const int quarter = warp & 3, half = warp >> 2;
-  constexpr int CW_EPI = N >= 32 ? N / 2 : N;
-  const int c_begin = half * CW_EPI, c_end = (N >= 32 || half == 0) ? c_begin + CW_EPI : c_begin;
+  // epilogue split: warp w reads TMEM lanes 32*(w%4).. (rows) and part w/4 of the columns
+  // (a quarter of them; with N = 16 the first four warps take all 16)
+  const int quarter = warp & 3, part = warp >> 2;
+  constexpr int CW_EPI = N >= 64 ? N / 4 : N;
+  const int c_begin = part * CW_EPI, c_end = (N >= 64 || part == 0) ? c_begin + CW_EPI : c_begin;
   for (; tile * TM < rows; tile += gridDim.x) {
     const long long m0 = tile * TM;
     asm volatile("cp.async.wait_all;" ::: "memory");
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(kUThreads, 1) umma_linear_kernel(const bf16u *
       if (row < rows && ok) {
         float z[16];
 #pragma unroll
-        for (int q = 0; q < 16; ++q) z[q] = __uint_as_float(r[q]) + (bias ? bias[c0 + q] : 0.f);
+        for (int q = 0; q < 16; ++q) z[q] = __uint_as_float(r[q]) + bias_s[c0 + q];
         if (Cf) {
           float4 *o = reinterpret_cast<float4 *>(Cf + (size_t)row * N + c0);
 #pragma unroll
@@ -223,7 +226,7 @@ __global__ void __launch_bounds__(kUThreads, 1) umma_linear_kernel(const bf16u *
 
 template <int N, int K>
 constexpr size_t u_shm() {
-  return (size_t)N * K * 2 + 128 * (size_t)K * 2 + 16;
+  return (size_t)N * K * 2 + 128 * (size_t)K * 2 + (size_t)N * 4 + 16;
 }
 
 template <int N, int K>
