@@ -73,7 +73,7 @@ def parse():
     p.add_argument("--train-samples", type=int, default=8_388_608)
     p.add_argument("--epochs", type=int, default=12)
     p.add_argument("--plain-only", action="store_true")
-    p.add_argument("--mlp-backend", choices=("mma.sync", "tcgen05"), default="mma.sync",
+    p.add_argument("--mlp-backend", choices=("mma.sync", "tcgen05"), default="tcgen05",
                    help="tensor-core path of the warm-start MLP (training and the step's inference)")
     p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
                    help="also time the step with the exact Newton Jacobian")
