@@ -401,6 +401,7 @@ int check_cells(pfchem_ctx *c, const pfchem_cells *cl) {
   if (!c || !cl) return fail(c, -1, "null argument");
   if (!c->has_net) return fail(c, -1, "pfchem_set_network has not been called");
   if (cl->ncells < 0) return fail(c, -1, "ncells < 0");
+  if (cl->ncells == 0) return 0;  // an empty batch (a rank without local cells) names no arrays
   const DevNet &n = c->net;
   if (!cl->temperature || !cl->saturation || !cl->den_kg || !cl->porosity || !cl->volume || !cl->pri_molal ||
       !cl->ionic_strength)
@@ -713,6 +714,10 @@ int pfchem_react_batch(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   int e = check_cells(c, cl);
   if (e) return e;
   if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  if (cl->ncells == 0) {
+    c->stats = pfchem_stats{};
+    return 0;
+  }
   if (!cl->total) return fail(c, -1, "total is null");
   cudaSetDevice(c->device);
   if (cl->on_device) return run_solve(c, device_args(cl, dt));
@@ -722,9 +727,13 @@ int pfchem_react_batch(pfchem_ctx *c, double dt, pfchem_cells *cl) {
 int pfchem_react_batch_interleaved(pfchem_ctx *c, double dt, int32_t ncomp, double *tran_xx, pfchem_cells *cl) {
   int e = check_cells(c, cl);
   if (e) return e;
-  if (!tran_xx) return fail(c, -1, "tran_xx is null");
   if (ncomp < c->net.N) return fail(c, -1, "ncomp %d < naqcomp %d", ncomp, c->net.N);
   if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  if (cl->ncells == 0) {
+    c->stats = pfchem_stats{};
+    return 0;
+  }
+  if (!tran_xx) return fail(c, -1, "tran_xx is null");
   cudaSetDevice(c->device);
   if (cl->on_device) {
     CellArgs a = device_args(cl, dt);
@@ -740,6 +749,7 @@ int pfchem_react_batch_interleaved(pfchem_ctx *c, double dt, int32_t ncomp, doub
 int pfchem_update_kinetic_state(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   int e = check_cells(c, cl);
   if (e) return e;
+  if (cl->ncells == 0) return 0;
   if (!cl->on_device) return fail(c, -1, "pfchem_update_kinetic_state takes device pointers");
   if (!cl->total) return fail(c, -1, "total is null");
   cudaSetDevice(c->device);
@@ -768,8 +778,12 @@ int pfchem_reserve(pfchem_ctx *c, int64_t ncells) {
 int pfchem_react_batch_async(pfchem_ctx *c, double dt, pfchem_cells *cl, void *stream) {
   int e = check_cells(c, cl);
   if (e) return e;
-  if (!cl->on_device) return fail(c, -1, "pfchem_react_batch_async takes device pointers");
+  if (!cl->on_device && cl->ncells) return fail(c, -1, "pfchem_react_batch_async takes device pointers");
   if (!(dt > 0.0)) return fail(c, -1, "dt must be > 0");
+  if (cl->ncells == 0) {
+    c->async_cells = 0;
+    return 0;
+  }
   if (!cl->total) return fail(c, -1, "total is null");
   cudaSetDevice(c->device);
   CellArgs a = device_args(cl, dt);
@@ -809,6 +823,7 @@ int pfchem_async_stats(pfchem_ctx *c, pfchem_stats *s) {
 int pfchem_reaction_blocks(pfchem_ctx *c, pfchem_cells *cl, pfchem_reaction_blocks_out *out) {
   int e = check_cells(c, cl);
   if (e) return e;
+  if (cl->ncells == 0) return 0;
   if (!cl->on_device) return fail(c, -1, "pfchem_reaction_blocks takes device pointers");
   if (!out || !out->res || !out->jac) return fail(c, -1, "res and jac are required");
   cudaSetDevice(c->device);
@@ -966,6 +981,7 @@ int pfchem_set_launch(pfchem_ctx *c, const pfchem_launch *l) {
 int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   int e = check_cells(c, cl);
   if (e) return e;
+  if (cl->ncells == 0) return 0;
   if (!cl->on_device) return fail(c, -1, "pfchem_autotune takes device pointers");
   cudaSetDevice(c->device);
   const DevNet &n = c->net;

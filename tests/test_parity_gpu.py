@@ -142,6 +142,49 @@ def test_inactive_cells_are_skipped(oracle):
     assert_parity(net, gpu, ref, mask=act)
 
 
+@pytest.mark.parametrize("ncells", [0, 1, 33])
+def test_small_and_ragged_batches(oracle, ncells):
+    """Batches of 0, 1 and 33 cells (not a multiple of a warp or a block):
+    an empty batch (a rank without local cells: no arrays at all, or empty
+    device arrays) returns 0; the others match the oracle on every cell."""
+    from pflotran_gb300.cells import CellBatch
+    net, opt, cells, dt = workloads.synthetic_cells(max(ncells, 1), seed=48)
+    step = ReactionStep(net, opt)
+    if ncells == 0:
+        assert step.react(CellBatch(0), dt) == 0
+        assert step.stats().ncells == 0
+        assert step.react(CellBatch.allocate(net, 0).to_device(), dt) == 0
+        return
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    assert np.array_equal(ref.status, gpu.status)
+    ok = ref.status == 0
+    assert_parity(net, gpu, ref, mask=ok & (ref.iterations == gpu.iterations))
+
+
+def test_nonfinite_and_all_inactive_cells(oracle):
+    """A cell whose totals are NaN stops with a non-converged status (the
+    kernels' finiteness checks and capped inner loops) while every other
+    cell of the batch matches the oracle; a batch with no active cell
+    returns every cell INACTIVE and unchanged."""
+    net, opt, cells, dt = workloads.calcite_cells(64, seed=49)
+    tot = cells.total.reshape(net.N, -1)
+    tot[:, 5] = np.nan
+    ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
+    assert gpu.status[5] != 0 and ref.status[5] != 0
+    rest = np.arange(64) != 5
+    assert (gpu.status[rest] == 0).all()
+    assert_parity(net, gpu, ref, mask=rest)
+    net, opt, cells, dt = workloads.calcite_cells(64, seed=50)
+    cells.active = np.zeros(64, np.int32)
+    before = cells.pri_molal.copy()
+    step = ReactionStep(net, opt)
+    d = cells.to_device()
+    assert step.react(d, dt) == 0
+    g = d.to_host()
+    assert (g.status == abi.CELL_INACTIVE).all()
+    assert np.array_equal(g.pri_molal, before)
+
+
 def test_alternative_guess_and_fallback(oracle):
     net, opt, cells, dt = workloads.synthetic_cells(2048, seed=8)
     ref, gpu, _ = run_both(oracle, net, opt, cells, dt)
