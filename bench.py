@@ -366,15 +366,18 @@ def timestepped(args, local):
     512 sampled cells per step."""
     from oracle import oracle
     from pflotran_gb300.os_run import OperatorSplitRun
+    from pflotran_gb300 import abi
     run = OperatorSplitRun(shape=(128, 128, 128), warm_start=True, autotune=False, drift_sample=512, log=None,
-                           device=f"cuda:{local}")
+                           device=f"cuda:{local}",
+                           mlp_backend=abi.MLP_TCGEN05 if args.mlp_backend == "tcgen05" else abi.MLP_MMA_SYNC)
     fn = lambda n_, o_, dt_, c_: oracle.react(n_, o_, dt_, c_, 0, os.cpu_count() or 1)
     recs = run.run(steps=50, oracle_fn=fn)
     react = [r["solves_per_s"] for r in recs if "solves_per_s" in r]
     worst = {k: max(r["drift"].get(k, 0.0) for r in recs) for k in ("pri_molal", "total", "mnrl_rate",
                                                                        "mnrl_volfrac")}
     return {"workload": "128^3 cells of the synthetic 12-species network, 50 steps of 1 day, upwind transport "
-                        f"({run.nsub} sub-steps) + reaction step with the learned warm start, one CUDA graph per step",
+                        f"({run.nsub} sub-steps) + reaction step with the learned warm start ({args.mlp_backend} "
+                        f"MLP), one CUDA graph per step",
             "steps": len(recs),
             "reaction_solves_per_s_mean": float(np.mean(react)) if react else None,
             "reaction_solves_per_s_first_last": [react[0], react[-1]] if react else None,
