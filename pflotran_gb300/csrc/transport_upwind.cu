@@ -12,14 +12,9 @@
 // with a0 = 1 - (dt_sub / V_pore) * (outgoing face flux) and a_f =
 // (dt_sub / V_pore) * (incoming flux through face f), 0 for outgoing and
 // closed faces.  The west neighbour of an x = 0 cell is the inflow water.
-// The coefficients are computed once per run.  A sub-step costs one
-// multiply per cell and component plus one FMA per incoming face (three of
-// the six faces in a mostly one-directional flow field): the FP64 pipe
-// bounds the kernel before HBM does, so faces whose coefficient is zero are
-// skipped -- decided once per cell from the coefficients' bit patterns, on
-// the integer pipe -- which leaves every result bit-identical to the full
-// seven-term sum for finite totals (an FMA with a zero coefficient returns
-// the accumulator unchanged).
+// The coefficients are computed once per run; a sub-step then costs one
+// multiply and six FMAs per cell and component on the FP64 pipe, which on
+// this part bounds the kernel before HBM does.
 //
 // Layout: T[c][x][y][z] (c slowest, z fastest); coef[k][x][y][z], k = a0,
 // aw, ae, as, an, ab, at.
@@ -47,18 +42,16 @@ __global__ void __launch_bounds__(256) upwind_step(const double *__restrict__ T,
   const long long os = y > 0 ? -sy : 0, on = y < ny - 1 ? sy : 0;
   const long long ob = z > 0 ? -1 : 0, ot = z < nz - 1 ? 1 : 0;
   const bool west_inflow = x == 0;
-  unsigned in = 0;  // bit k-1: face k has a non-zero (incoming) coefficient
-#pragma unroll
-  for (int k = 1; k < 7; ++k) in |= ((__double_as_longlong(a[k]) << 1) != 0 ? 1u : 0u) << (k - 1);
   for (int c = 0; c < ncomp; ++c) {
     const double *Tc = T + c * n + cell;
     double acc = a[0] * Tc[0];
-    if (in & 1u) acc = fma(a[1], west_inflow ? inflow[c] : Tc[ow], acc);
-    if (in & 2u) acc = fma(a[2], Tc[oe], acc);
-    if (in & 4u) acc = fma(a[3], Tc[os], acc);
-    if (in & 8u) acc = fma(a[4], Tc[on], acc);
-    if (in & 16u) acc = fma(a[5], Tc[ob], acc);
-    if (in & 32u) acc = fma(a[6], Tc[ot], acc);
+    const double tw = Tc[ow];
+    acc = fma(a[1], west_inflow ? inflow[c] : tw, acc);
+    acc = fma(a[2], Tc[oe], acc);
+    acc = fma(a[3], Tc[os], acc);
+    acc = fma(a[4], Tc[on], acc);
+    acc = fma(a[5], Tc[ob], acc);
+    acc = fma(a[6], Tc[ot], acc);
     Tn[c * n + cell] = acc;
   }
 }
