@@ -468,11 +468,11 @@ int pfchem_autotune(pfchem_ctx *ctx, double dt, pfchem_cells *cells);
  * than the previous-step guess's.  All pointers are device pointers. */
 #define PFCHEM_SURROGATE_FEATURES 16
 /* Tensor-core path of the network's dense layers (training and inference):
- * MMA_SYNC = warp-level mma.sync (and the fused one-kernel inference, the
- * default); TCGEN05 = tcgen05.mma with FP32 accumulators in tensor memory,
- * each layer's weights resident in shared memory, a fused bias/GELU
- * epilogue, layer by layer (the weight gradients stay split-K mma.sync).
- * Call before training or between steps.  No counterpart in the reference. */
+ * TCGEN05 (the default) = tcgen05.mma with FP32 accumulators in tensor
+ * memory, each layer's weights resident in shared memory, a fused bias/GELU
+ * epilogue, layer by layer (the weight gradients stay split-K mma.sync);
+ * MMA_SYNC = warp-level mma.sync and the fused one-kernel inference.  Call
+ * before training or between steps.  No counterpart in the reference. */
 #define PFCHEM_MLP_MMA_SYNC 0
 #define PFCHEM_MLP_TCGEN05 1
 int pfchem_surrogate_backend(pfchem_ctx *ctx, int backend);

@@ -514,7 +514,7 @@ struct Surrogate {
   float *ws = nullptr;      // split-K partials of the weight gradients (kSplits x 256 x 256)
   // tensor-core path of the dense layers: 0 = mma.sync (warp-level MMA, the
   // fused one-kernel inference), 1 = tcgen05.mma with tensor-memory accumulators
-  int backend = 0;
+  int backend = 1;  // tcgen05 (PFCHEM_MLP_TCGEN05) unless the caller picks mma.sync
   int *uerr = nullptr;      // set by a tcgen05 kernel whose wait ran out
   bf16 *ubpk = nullptr;     // a layer's weights packed for the tcgen05 kernels (256 x 256)
   int sms = 0;

@@ -252,7 +252,7 @@ class OperatorSplitRun:
     def __init__(self, shape=(128, 128, 128), dt=86400.0, sigma=1.5, corr_len=10.0, seed=11, warm_start=True,
                  train_samples=2_097_152, epochs=8, autotune=True, drift_sample=512,
                  cells_per_step=2.0, courant=0.9, device="cuda", log=print, jacobian=0, transport="cuda",
-                 mlp_backend=0):
+                 mlp_backend=None):
         import torch
         from . import workloads
         from .lib import ReactionStep
@@ -277,7 +277,8 @@ class OperatorSplitRun:
         d.total_out.copy_(d.total)  # transport reads the previous step's aqueous totals
         self.cells = d
         self.step = ReactionStep(net, self.opt)
-        self.step.surrogate_backend(mlp_backend)  # PFCHEM_MLP_*: tensor-core path of the warm start
+        if mlp_backend is not None:  # PFCHEM_MLP_*: tensor-core path of the warm start (library default: tcgen05)
+            self.step.surrogate_backend(mlp_backend)
         self.report = {"train": None}
         if warm_start:
             t0 = time.perf_counter()

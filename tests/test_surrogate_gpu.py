@@ -5,7 +5,7 @@ import pytest
 
 from oracle import mlp_oracle as mo
 from oracle import parity
-from pflotran_gb300 import workloads
+from pflotran_gb300 import abi, workloads
 from pflotran_gb300.lib import ReactionStep
 from pflotran_gb300.surrogate import fit, generate
 
@@ -24,6 +24,7 @@ def test_gradients_match_fp64_oracle():
     net = workloads.synthetic_network()
     _, opt, _, _ = workloads.synthetic_cells(8, seed=1, net=net)
     step = ReactionStep(net, opt)
+    step.surrogate_backend(abi.MLP_MMA_SYNC)  # the tcgen05 path has its own gradient test
     X, molal = _data(step, 1024, 31)
     Xh = X.cpu().numpy().astype(np.float64)
     fm = Xh.mean(0)
@@ -60,6 +61,7 @@ def test_fused_inference_equals_layer_by_layer():
     net = workloads.synthetic_network()
     _, opt, _, _ = workloads.synthetic_cells(8, seed=1, net=net)
     step = ReactionStep(net, opt)
+    step.surrogate_backend(abi.MLP_MMA_SYNC)
     X, molal = _data(step, 65536, 43)
     fit(step, X, molal, epochs=2, batch=4096)
     _, _, cells, _ = workloads.synthetic_cells(50001, seed=44, net=net)

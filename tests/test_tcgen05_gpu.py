@@ -26,6 +26,7 @@ def test_tcgen05_layers_match_mma_sync_layers():
     net = workloads.synthetic_network()
     _, opt, _, _ = workloads.synthetic_cells(8, seed=1, net=net)
     step = ReactionStep(net, opt)
+    step.surrogate_backend(abi.MLP_MMA_SYNC)
     X, molal = _data(step, 65536, 43)
     fit(step, X, molal, epochs=2, batch=4096)
     _, _, cells, _ = workloads.synthetic_cells(50001, seed=44, net=net)
