@@ -254,7 +254,8 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": f"synthetic 12-species network (40 complexes, 6 minerals, 4 ion-exchange, "
-                               f"2 surface-complexation), {args.ncells} cells, dt 1 day, 1e-12 rel. residual",
+                               f"2 surface-complexation), {args.ncells} cells, dt 1 day, 1e-12 rel. residual, "
+                               f"exact_jacobian_after {opt.exact_jacobian_after} (the options of the GPU arm)",
                    "sample_cells_per_step": n},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{n} of {args.ncells} cells per step, drawn at random (seed {SAMPLE_SEED}); "
