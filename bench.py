@@ -418,15 +418,22 @@ def main():
     step.surrogate_backend(mlp_backend)
     pristine = host.to_device()
     dev = pristine.copy()
-    tune = None
-    if args.autotune:
-        # the launch search runs on its own draw of the workload
+    def autotune():
+        # the launch search runs on its own draw of the workload, on the
+        # step as it is configured (plain, or with the warm start enabled)
         _, _, th, _ = make_workload(min(262144, n), device=f"cuda:{local}", rank=rank, seed=4049)
         t0 = time.perf_counter()
         step.autotune(th.to_device(), dt)
-        tune = {"cells": th.ncells, "s": time.perf_counter() - t0}
-        del th
+        return {"cells": th.ncells, "s": time.perf_counter() - t0}
+
+    def launch_dict(L, tune):
+        return {"block_threads": L.block_threads, "blocks_per_sm": L.blocks_per_sm,
+                "refill_min_idle": L.refill_min_idle, "variant": L.variant,
+                "source": "pfchem_autotune" if tune else "library default", "autotune": tune}
+
+    tune = autotune() if args.autotune else None
     launch = step.launch()
+    plain_launch = launch_dict(launch, tune)
 
     def restore():
         for f in CellBatch.FIELDS:
@@ -524,6 +531,10 @@ def main():
             step.surrogate_backend(mlp_backend)
         inference["backend_in_step"] = args.mlp_backend
         step.surrogate_enable(True)
+        if args.autotune:
+            # the warm step has its own best launch (fewer iterations per cell)
+            tune = autotune()
+            launch = step.launch()
         warm = dict(report=rep, t_gen=t_gen, t_fit=t_fit, inference=inference,
                     err_rms=float(err.pow(2).mean().sqrt()), err_p50=float(err.max(0).values.median()),
                     err0_rms=float(err0.pow(2).mean().sqrt()), err0_p50=float(err0.max(0).values.median()))
@@ -633,6 +644,7 @@ def main():
     if warm is not None:
         r = warm["report"]
         wline = {"plain_value": plain["value"], "plain_ms_per_step": plain["total_ms"] / args.steps,
+                 "plain_launch": plain_launch,
                  "plain_mean_newton_iterations": float(np.mean(plain["iters"])) / n,
                  "plain_nonconverged": plain["nonconverged"],
                  "plain_lane_efficiency": plain["eff"], "plain_queue_drain_ms": plain["drain_ms"],
@@ -657,9 +669,7 @@ def main():
                                f"previous-step guess, 1e-12 rel. residual, exact_jacobian_after "
                                f"{opt.exact_jacobian_after}; converged cells counted",
                    "ncells": n, "l2": "inputs ~1.3 GB >> L2; state restored from a pristine copy between steps",
-                   "launch": {"block_threads": launch.block_threads, "blocks_per_sm": launch.blocks_per_sm,
-                              "refill_min_idle": launch.refill_min_idle, "variant": launch.variant,
-                              "source": "pfchem_autotune" if tune else "library default", "autotune": tune},
+                   "launch": launch_dict(launch, tune),
                    "parallelism": "replicas" if world > 1 else "single"},
         "mean_newton_iterations": mean_iters, "converged_cells": int((g.status == 0).sum()),
         "nonconverged": head["nonconverged"],
