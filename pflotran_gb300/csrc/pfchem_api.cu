@@ -476,6 +476,14 @@ int enqueue_step(pfchem_ctx *c, const CellArgs &a, bool predict, cudaStream_t st
   const int grid = std::max(1, c->num_sms * L.blocks_per_sm);
   if (!scr) scr = c->scratch;
   if (!prep) prep = c->prep;
+  // the generated kernel is compiled for one block size and shared-memory
+  // layout (its per-thread stride and the dynamic shared memory it expects):
+  // never launch it with another
+  if (is_specialized(L.variant) &&
+      (!c->gen_fn || c->gen_block != L.block_threads ||
+       c->gen_compact != (L.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT)))
+    return fail(c, -1, "launch (%d threads, %s layout) does not match the loaded specialized kernel",
+                L.block_threads, L.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT ? "compact" : "augmented");
   cudaError_t me = cudaMemsetAsync(scr, 0, sizeof(Scratch), st);
   if (me != cudaSuccess) return fail(c, -2, "statistics reset: %s", cudaGetErrorString(me));
   cudaError_t pe =
@@ -1039,8 +1047,14 @@ int pfchem_autotune(pfchem_ctx *c, double dt, pfchem_cells *cl) {
   std::vector<std::pair<double, pfchem_launch>> timed;
   int rc = 0;
   auto time_launch = [&](const pfchem_launch &l, int reps) {
-    c->launch = l;
     double ms = 1e30;
+    // load the generated kernel this launch was compiled for
+    if (is_specialized(l.variant) &&
+        ensure_gen(c, l.block_threads, l.variant == PFCHEM_KERNEL_SPECIALIZED_COMPACT) < 1) {
+      rc = -2;
+      return ms;
+    }
+    c->launch = l;
     for (int rep = 0; rep < reps; ++rep) {
       rc = pfchem_react_batch(c, dt, cl);
       if (rc < 0) break;
