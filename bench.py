@@ -73,6 +73,8 @@ def parse():
     p.add_argument("--train-samples", type=int, default=8_388_608)
     p.add_argument("--epochs", type=int, default=12)
     p.add_argument("--plain-only", action="store_true")
+    p.add_argument("--launch", default=None, metavar="THREADS,BLOCKS_PER_SM,REFILL,VARIANT",
+                   help="a fixed launch for every step (pfchem_set_launch) instead of the tuner's")
     p.add_argument("--mlp-backend", choices=("mma.sync", "tcgen05"), default="tcgen05",
                    help="tensor-core path of the warm-start MLP (training and the step's inference)")
     p.add_argument("--exact-jacobian", action=argparse.BooleanOptionalAction, default=True,
@@ -431,6 +433,9 @@ def main():
                 "refill_min_idle": L.refill_min_idle, "variant": L.variant,
                 "source": "pfchem_autotune" if tune else "library default", "autotune": tune}
 
+    if args.launch:
+        args.autotune = False
+        step.set_launch(*[int(x) for x in args.launch.split(",")])
     tune = autotune() if args.autotune else None
     launch = step.launch()
     plain_launch = launch_dict(launch, tune)
