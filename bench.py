@@ -688,8 +688,7 @@ def main():
                      "frac": achieved_tflops / probe if probe else None,
                      "traffic": TRAFFIC_BYTES_PER_CELL * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pfchem_gen_react "
-                                       "launch on 524288 cells, scaled by cells "
-                                       "(profiles/pfchem_gen_react_synthetic12_524k.md)",
+                                       "launch on 524288 cells of this workload (plain step), scaled by cells",
                      "peak_source": "measured DFMA throughput on this GPU (pfchem_probe_fp64_peak, FMA = 2 flops)",
                      "flops_per_step": flops,
                      "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
