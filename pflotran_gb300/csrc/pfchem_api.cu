@@ -374,21 +374,39 @@ int ensure_gen(pfchem_ctx *c, int block, bool compact) {
   return nb;
 }
 
-// Specialized kernel (augmented layout), 32 threads per block, as many
-// blocks per SM as fit, refill as soon as one lane of a warp is idle (the
-// prologue leaves a refill only loads to do; the autotuner's usual choice,
-// +5-7% over refilling at 8 idle lanes at 2M cells of the 12-species
-// network).  The compact layout fits one more block per SM for that network
-// but measured 1-4% slower (its unrolled elimination costs more than the
-// extra warp gains); the autotuner tries both.
+// Specialized kernel, 32 threads per block, as many blocks per SM as fit,
+// refill as soon as one lane of a warp is idle (the prologue leaves a
+// refill only loads to do; +5-7% over refilling at 8 idle lanes at 2M cells
+// of the 12-species network).  The compact layout (J alone in shared memory,
+// the right-hand side in registers) when it fits more blocks per SM than the
+// augmented one: for that network 6 blocks against 5, 273 vs 286 ms per
+// plain step and 207 vs 218 ms per warm step, the same arithmetic in the
+// same order; otherwise the augmented layout.  The autotuner tries both.
 int default_specialized_launch(pfchem_ctx *c) {
   const int block = 32;
-  int nb = ensure_gen(c, block, false);
-  if (nb < 1) return -2;
+  {  // both layouts compiled concurrently (NVRTC), then loaded from the cache
+    std::vector<std::pair<int, bool>> cands{{block, false}};
+    if (gen_shared_bytes(c->net, block, true) <= 227 * 1024) cands.push_back({block, true});
+    std::string err;
+    if (gen_kernels_prepare(c->net, cands, &err)) return fail(c, -2, "specialized kernel: %s", err.c_str());
+  }
+  const int nb_aug = ensure_gen(c, block, false);
+  if (nb_aug < 1) return -2;
+  bool compact = false;
+  int nb = nb_aug;
+  if (gen_shared_bytes(c->net, block, true) <= 227 * 1024) {
+    const int nb_cmp = ensure_gen(c, block, true);
+    if (nb_cmp > nb_aug) {
+      compact = true;
+      nb = nb_cmp;
+    } else if (ensure_gen(c, block, false) < 1) {
+      return -2;
+    }
+  }
   c->launch.block_threads = block;
   c->launch.blocks_per_sm = nb;
   c->launch.refill_min_idle = 1;
-  c->launch.variant = PFCHEM_KERNEL_SPECIALIZED;
+  c->launch.variant = compact ? PFCHEM_KERNEL_SPECIALIZED_COMPACT : PFCHEM_KERNEL_SPECIALIZED;
   return 0;
 }
 

@@ -874,9 +874,11 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
   void solve() {
     if (compact) {
       // J alone in shared memory: the right-hand side stays in registers
-      // (pivot-column and row loops unrolled so every f index is a constant),
-      // the row exponents are 16-bit.  The same operations in the same
-      // order as the augmented form below.
+      // (the row loops unrolled under an i > j predicate so every f index is
+      // a constant, the pivot column rolled to keep the code small; f[j] and
+      // the pivot swap read through unrolled selects), the row exponents are
+      // 16-bit.  The same operations in the same order as the augmented form
+      // below.
       o << R"(__device__ __forceinline__ bool lu_solve(double *Jb, unsigned short *Eb, double (&f)[NP]) {
 #define JA(i, k) Jb[((i) * NP + (k)) * JS]
 #pragma unroll 1
@@ -886,11 +888,11 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
     if (r == 0) return false;
     Eb[i * JS] = (unsigned short)((r & 0x7FF0000000000000LL) >> 48);
   }
-#pragma unroll
+#pragma unroll 1
   for (int j = 0; j < NP; ++j) {
     int p = j;
     long long best = absbits(JA(j, j)) - ((long long)Eb[j * JS] << 48);
-#pragma unroll
+#pragma unroll 1
     for (int i = j + 1; i < NP; ++i) {
       const long long kk = absbits(JA(i, j)) - ((long long)Eb[i * JS] << 48);
       if (kk >= best) { best = kk; p = i; }
@@ -899,20 +901,27 @@ __device__ __noinline__ double xlog(double x) { return log(x); }
 #pragma unroll 1
       for (int k = j; k < NP; ++k) { const double t = JA(p, k); JA(p, k) = JA(j, k); JA(j, k) = t; }
       const unsigned short te = Eb[p * JS]; Eb[p * JS] = Eb[j * JS]; Eb[j * JS] = te;
+      double fp = f[0], fq = f[0];
 #pragma unroll
-      for (int i = j + 1; i < NP; ++i)
-        if (p == i) { const double t = f[i]; f[i] = f[j]; f[j] = t; }
+      for (int q = 1; q < NP; ++q) { if (q == p) fp = f[q]; if (q == j) fq = f[q]; }
+#pragma unroll
+      for (int q = 0; q < NP; ++q) { if (q == j) f[q] = fp; else if (q == p) f[q] = fq; }
     }
     double piv = JA(j, j);
     if (piv == 0.0) piv = 1e-20;
     const double ip = 1.0 / piv;
     JA(j, j) = ip;
+    double fj = f[0];
 #pragma unroll
-    for (int i = j + 1; i < NP; ++i) {
-      const double l = JA(i, j) * ip;
+    for (int q = 1; q < NP; ++q) if (q == j) fj = f[q];
+#pragma unroll
+    for (int i = 1; i < NP; ++i) {
+      if (i > j) {
+        const double l = JA(i, j) * ip;
 #pragma unroll 1
-      for (int k = j + 1; k < NP; ++k) JA(i, k) = fma(-l, JA(j, k), JA(i, k));
-      f[i] = fma(-l, f[j], f[i]);
+        for (int k = j + 1; k < NP; ++k) JA(i, k) = fma(-l, JA(j, k), JA(i, k));
+        f[i] = fma(-l, fj, f[i]);
+      }
     }
   }
 #pragma unroll
