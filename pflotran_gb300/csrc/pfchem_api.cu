@@ -378,10 +378,11 @@ int ensure_gen(pfchem_ctx *c, int block, bool compact) {
 // refill as soon as one lane of a warp is idle (the prologue leaves a
 // refill only loads to do; +5-7% over refilling at 8 idle lanes at 2M cells
 // of the 12-species network).  The compact layout (J alone in shared memory,
-// the right-hand side in registers) when it fits more blocks per SM than the
-// augmented one: for that network 6 blocks against 5, 273 vs 286 ms per
-// plain step and 207 vs 218 ms per warm step, the same arithmetic in the
-// same order; otherwise the augmented layout.  The autotuner tries both.
+// the right-hand side in registers) whenever it fits as many blocks per SM
+// as the augmented one: for that network 6 blocks against 5, 273 vs 286 ms
+// per plain step and 207 vs 218 ms per warm step; 4 % faster at equal
+// residency on the calcite and 16-species networks; the same arithmetic in
+// the same order.  The autotuner tries both.
 int default_specialized_launch(pfchem_ctx *c) {
   const int block = 32;
   {  // both layouts compiled concurrently (NVRTC), then loaded from the cache
@@ -396,7 +397,7 @@ int default_specialized_launch(pfchem_ctx *c) {
   int nb = nb_aug;
   if (gen_shared_bytes(c->net, block, true) <= 227 * 1024) {
     const int nb_cmp = ensure_gen(c, block, true);
-    if (nb_cmp > nb_aug) {
+    if (nb_cmp >= nb_aug) {
       compact = true;
       nb = nb_cmp;
     } else if (ensure_gen(c, block, false) < 1) {
