@@ -429,10 +429,12 @@ typedef struct pfchem_launch {
   int32_t refill_min_idle;  /* lanes idle in a warp before they fetch new cells */
   int32_t variant;          /* PFCHEM_KERNEL_* */
 } pfchem_launch;
-#define PFCHEM_KERNEL_SPECIALIZED 0 /* network-specialized kernel compiled at set_network (default) */
+#define PFCHEM_KERNEL_SPECIALIZED 0 /* network-specialized kernel compiled at set_network, [J | F] in
+                                       shared memory */
 #define PFCHEM_KERNEL_GENERIC 1     /* table-driven kernel compiled into the library */
 #define PFCHEM_KERNEL_SPECIALIZED_COMPACT 2 /* specialized, J alone in shared memory (right-hand
-                                               side in registers): fits more blocks per SM, same results */
+                                               side in registers): fits more blocks per SM, same results;
+                                               the default wherever it fits as many blocks as variant 0 */
 /* Cooperative kernels: 8, 16 or 32 lanes solve one cell together (species,
  * complexes, Jacobian entries, sorption sites, minerals and LU rows spread
  * over the lanes; the cell's system in shared memory once per group).  Not
