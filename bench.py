@@ -53,9 +53,10 @@ sys.path.insert(0, ROOT)
 METRIC = "converged cell chemistry solves/s at 1e-12 rel. residual, warm-start vs plain GPU Newton"
 UNIT = "cell solves/s"
 NCELLS = 2_097_152
-# DRAM bytes per cell of the solve kernel, from an ncu capture of one launch
-# on 524,288 cells of the same workload (568.3 MB read + 314.2 MB written)
-TRAFFIC_BYTES_PER_CELL = (568272896 + 314241024) / 524288
+# DRAM bytes per cell of the solve kernel, from an ncu capture of one warm-step
+# launch on 524,288 cells of the same workload, default compact launch
+# (625.0 MB read + 410.6 MB written)
+TRAFFIC_BYTES_PER_CELL = (625028864 + 410648320) / 524288
 SAMPLE_SEED = 12345
 
 
@@ -688,7 +689,8 @@ def main():
                      "frac": achieved_tflops / probe if probe else None,
                      "traffic": TRAFFIC_BYTES_PER_CELL * n,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one pfchem_gen_react "
-                                       "launch on 524288 cells of this workload (plain step), scaled by cells",
+                                       "launch on 524288 cells of this workload (warm step, compact layout), "
+                                       "scaled by cells",
                      "peak_source": "measured DFMA throughput on this GPU (pfchem_probe_fp64_peak, FMA = 2 flops)",
                      "flops_per_step": flops,
                      "hbm": {"achieved": hbm_gbs, "peak": hbm_peak, "unit": "GB/s", "frac": hbm_gbs / hbm_peak,
