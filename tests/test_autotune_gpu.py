@@ -43,3 +43,29 @@ def test_autotuned_launch_is_no_slower_and_bit_identical():
         assert ok.mean() > 0.98
         errs = compare(net, b, a, mask=ok)
         assert all(v <= 1e-10 for v in errs.values()), errs
+
+
+@pytest.mark.parametrize("kind", ["calcite", "synthetic"])
+def test_shared_memory_layouts_are_bit_identical(kind):
+    """The specialized kernel's two shared-memory layouts (the augmented
+    [J | F], and the compact J with the right-hand side in registers and the
+    pivot-column loop of the elimination rolled) and block sizes of 32 and
+    64 threads do the same operations per cell: every output agrees bit for
+    bit."""
+    if kind == "calcite":
+        net, opt, cells, dt = workloads.calcite_cells(8192, seed=79, temperature_dependent=True)
+    else:
+        net, opt, cells, dt = workloads.synthetic_cells(8192, seed=80)
+    step = ReactionStep(net, opt)
+    outs = []
+    for block, variant in ((32, abi.KERNEL_SPECIALIZED), (32, abi.KERNEL_SPECIALIZED_COMPACT),
+                           (64, abi.KERNEL_SPECIALIZED_COMPACT)):
+        step.set_launch(block, 1, 1, variant)
+        d = cells.to_device()
+        step.react(d, dt)
+        outs.append(d.to_host())
+    for o in outs[1:]:
+        for f in ("pri_molal", "total_out", "mnrl_rate", "mnrl_volfrac", "total_sorb_eq", "ionic_strength",
+                  "iterations", "status"):
+            if getattr(o, f) is not None:
+                np.testing.assert_array_equal(getattr(outs[0], f), getattr(o, f), err_msg=f)
